@@ -1,0 +1,443 @@
+// Per-particle SDE steps of the four heliospheric transport models.
+//
+// Each step restates the reference GPU kernels' equations (paths relative to
+// the reference project):
+//   2D Geliosphere   CUDAKernel/src/GeliosphereModel.cu:82-390
+//   2D SolarProp     CUDAKernel/src/SolarPropLikeModel.cu:95-247
+//   1D B-p           CUDAKernel/src/OneDimensionBpModel.cu:69-140
+//   1D F-p           CUDAKernel/src/OneDimensionFpModel.cu:73-141
+// in a form arranged for sm_103a:
+//   * kinetic energy and rigidity in GeV / GV instead of SI (the reference's
+//     FP32 T0^2 q^2 1e18 intermediates sit next to FLT_MIN); the kinetic
+//     energy from momentum uses P^2 / (sqrt(T0^2 + P^2) + T0), which is the
+//     reference's sqrt(T0^2 + P^2) - T0 without the cancellation;
+//   * powf(Cb, 1.5 / 2.5 / 3) become products of Cb and one sqrt; repeated
+//     divisions become multiplications by a handful of reciprocals;
+//   * the FP32 state (r, theta, T, p, sumac) is updated with Kahan
+//     compensation, so tens of thousands of steps do not accumulate rounding;
+//   * the noise terms with coefficients that are identically zero in the
+//     reference (B13 = B23 = 0 because Krph = Ktph = 0) are not evaluated.
+// The same templates are instantiated in FP64 (the FP64-step variant).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gelio {
+
+// ---------------------------------------------------------------------------
+// Constants, with the values and FP32 arithmetic of CosmicConstants.cu:14-41.
+// ---------------------------------------------------------------------------
+constexpr float kPi = 3.141592654f;
+constexpr float kT0 = (float)(1.67261e-27 * 2.99793e8 * 2.99793e8 / (1.60219e-19 * 1e9));
+constexpr float kOmega = 2.866e-6f;
+constexpr float kA = 3.4f;
+constexpr float kKonvF = 9.0e-5f / 2.0f;
+constexpr float kRh = 0.0046367333333333f;
+constexpr float kThetaLo = 1.7f * kPi / 180.0f;    // GeliosphereModel.cu:97
+constexpr float kThetaHi = 178.3f * kPi / 180.0f;
+constexpr float kC53 = 5.0f / 3.4f;
+constexpr float kTwoPi = 2.0f * kPi;
+// SolarPropLikeModel.cu:213 uses the fixed constant of CosmicConstants.cu:37.
+constexpr float kDriftThetaConstantSP = -1.0f * 1.0f * (9.0e-5f / 2.0f) * (2.0f / (3.0f * 3.4f));
+
+// Model ids (match GELIO_MODEL_* in gelio.h).
+constexpr int kModelFp = 0;
+constexpr int kModelBp = 1;
+constexpr int kModelSolarProp = 2;
+constexpr int kModelGeliosphere = 3;
+
+// ---------------------------------------------------------------------------
+// Precision policy.
+// ---------------------------------------------------------------------------
+template <class R> struct Math;
+
+template <> struct Math<float> {
+  static constexpr bool kCompensate = true;
+  __device__ static __forceinline__ float sqrt(float x) { return sqrtf(x); }
+  __device__ static __forceinline__ float rcp(float x) { return __fdividef(1.0f, x); }
+  __device__ static __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
+  __device__ static __forceinline__ void sincos(float x, float *s, float *c) { sincosf(x, s, c); }
+  __device__ static __forceinline__ float sin(float x) { return sinf(x); }
+  __device__ static __forceinline__ float acos(float x) { return acosf(x); }
+  __device__ static __forceinline__ float atan(float x) { return atanf(x); }
+  __device__ static __forceinline__ float abs(float x) { return fabsf(x); }
+};
+
+template <> struct Math<double> {
+  static constexpr bool kCompensate = false;
+  __device__ static __forceinline__ double sqrt(double x) { return ::sqrt(x); }
+  __device__ static __forceinline__ double rcp(double x) { return 1.0 / x; }
+  __device__ static __forceinline__ double div(double a, double b) { return a / b; }
+  __device__ static __forceinline__ void sincos(double x, double *s, double *c) { ::sincos(x, s, c); }
+  __device__ static __forceinline__ double sin(double x) { return ::sin(x); }
+  __device__ static __forceinline__ double acos(double x) { return ::acos(x); }
+  __device__ static __forceinline__ double atan(double x) { return ::atan(x); }
+  __device__ static __forceinline__ double abs(double x) { return fabs(x); }
+};
+
+// Kahan-compensated scalar: value v, running compensation c (true ~ v - c).
+template <class R> struct Acc {
+  R v, c;
+  __device__ __forceinline__ void set(R x) { v = x; c = R(0); }
+  __device__ __forceinline__ void add(R d) {
+    if constexpr (Math<R>::kCompensate) {
+      const R y = d - c;
+      const R t = v + y;
+      c = (t - v) - y;
+      v = t;
+    } else {
+      v += d;
+    }
+  }
+  __device__ __forceinline__ void negate() { v = -v; c = -c; }
+};
+
+// Raw parameters of one simulation (device copy of gelio_sim_params, resolved).
+struct SimDev {
+  float K0, V, dt, r_inj, theta_inj, tilt, polarity, ratio, delta0;
+  float injection_max, inj_min, inj_max;
+  int model, injection, inj_points, flags;
+  float grid_min, grid_max;
+  int grid_bins;
+  int grid_is_points;        // grid bin = LOG_GRID point index
+  uint32_t key0, key1;       // Philox key
+  long long n_particles;
+  double grid_log_lo, grid_inv_dlog;
+};
+
+// Per-lane constants of the current particle's simulation, in precision R.
+template <class R> struct Consts {
+  R V, dt, sqdt, K0, ratio, one_m_ratio, delta0, alphaM;
+  R ov, ov2;          // omega / V and its square
+  R kpar_c;           // K0 * (5/3.4) / 3
+  R kd_c;             // K0 / (3 * (5/3.4))
+  R inv_3c53;         // 1 / (3 * (5/3.4))
+  R d0rh2;            // delta0^2 / rh^2
+  R drift2;           // polarity * konvF * 2 / (3A)
+  R drift1;           // polarity * konvF * 1 / (3A)
+  R dtheta_sp;        // SolarProp theta drift constant
+  R adv;              // 1D: (2/3) V dt; 2D: (2/3) V dt as well
+};
+
+template <class R>
+__device__ __forceinline__ void make_consts(const SimDev &s, Consts<R> &k) {
+  using M = Math<R>;
+  const R V = (s.model == kModelBp) ? -(R)s.V : (R)s.V;   // CosmicConstants.cu:73-83
+  k.V = V;
+  k.dt = (R)s.dt;
+  k.sqdt = M::sqrt(k.dt);
+  k.K0 = (R)s.K0;
+  k.ratio = (R)s.ratio;
+  k.one_m_ratio = R(1) - k.ratio;
+  k.delta0 = (R)s.delta0;
+  k.alphaM = (R)s.tilt;
+  k.ov = M::div((R)kOmega, V);
+  k.ov2 = k.ov * k.ov;
+  k.kpar_c = k.K0 * (R)kC53 * M::rcp(R(3));
+  k.kd_c = M::div(k.K0, R(3) * (R)kC53);
+  k.inv_3c53 = M::rcp(R(3) * (R)kC53);
+  k.d0rh2 = M::div(k.delta0 * k.delta0, (R)kRh * (R)kRh);
+  k.drift2 = (R)s.polarity * (R)kKonvF * M::div(R(2), R(3) * (R)kA);
+  k.drift1 = (R)s.polarity * (R)kKonvF * M::div(R(1), R(3) * (R)kA);
+  k.dtheta_sp = (s.flags & 1) ? -(R)s.polarity * (R)kKonvF * M::div(R(2), R(3) * (R)kA)
+                              : (R)kDriftThetaConstantSP;
+  k.adv = R(2) * V * k.dt * M::rcp(R(3));
+}
+
+// ---------------------------------------------------------------------------
+// Injection energies (GeV, FP32 exactly as specified so the oracle can
+// reproduce them bit for bit).
+// ---------------------------------------------------------------------------
+
+// CosmicUtils.cu:17-34 with injectionMax * quantityPerEnergy computed in FP32
+// and the integer parts taken exactly (the reference's float division is exact
+// for the particle indices below 2^24 it is used with).
+__device__ __forceinline__ float inj_reference_uniform(unsigned long long s, float injection_max) {
+  const float mq = __fmul_rn(injection_max, 10000.0f);
+  const unsigned long long m = (unsigned long long)mq;
+  if ((float)s > mq && m > 0ull) s -= (s / m) * m;
+  const unsigned long long mod = (s >= 10000ull) ? s / 10000ull : 0ull;
+  const float frac = __fdiv_rn((float)(s - mod * 10000ull + 1ull), 10000.0f);
+  return __fadd_rn((float)mod, frac);
+}
+
+// Constants.hpp:234-239 (the CPU models' grid): from + (id mod 1e4) * step.
+__device__ __forceinline__ float inj_cpu_uniform(unsigned long long s, float injection_max) {
+  const double step = ((double)injection_max - 0.0001) / 10000.0;
+  return (float)(0.0001 + (double)(s % 10000ull) * step);
+}
+
+__device__ __forceinline__ float inj_solarprop(unsigned long long s, const float *sp30) {
+  return sp30[(int)(s % 30ull)];
+}
+
+// ---------------------------------------------------------------------------
+// Lane state.
+// ---------------------------------------------------------------------------
+template <class R> struct Lane {
+  Acc<R> r, th, T, P, sumac;
+  float Tinj;
+  uint32_t steps;
+  int sim;
+  int gbin;
+  unsigned long long pid;
+  uint32_t key0, key1;
+};
+
+// Outcome of one step.
+enum StepResult : int { kContinue = 0, kRecordAndStop = 1, kStop = 2, kRecordAndContinue = 3 };
+
+// ---------------------------------------------------------------------------
+// 2D Geliosphere: GeliosphereModel.cu:82-390 (Eq. 16-44 of the Geliosphere
+// model description, drifts of Kappl 2016 Eq. 26-37).
+// ---------------------------------------------------------------------------
+template <class R>
+__device__ __forceinline__ int step_geliosphere(Lane<R> &L, const Consts<R> &k, R n1, R n2, R n4) {
+  using M = Math<R>;
+  const R r = L.r.v, th = L.th.v, T = L.T.v;
+  const R T0 = (R)kT0;
+  const R Tp = T + T0;
+  const R T2 = Tp + T0;
+  const R P = M::sqrt(T * T2);               // rigidity [GV]
+  const R inv_Tp = M::rcp(Tp);
+  const R beta = P * inv_Tp;
+  R s, c;
+  M::sincos(th, &s, &c);
+  const R inv_s = M::rcp(s);
+  const bool polarA = (th < (R)kThetaLo) || (th > (R)kThetaHi);   // Eq. 25 branch
+  const bool nonpolarB = (th > (R)kThetaLo) && (th < (R)kThetaHi);
+  const R inv_rh = R(1) / (R)kRh;
+  const R delta = polarA ? (R)0.003f : k.delta0 * inv_s;
+  const R deltarh = delta * inv_rh;
+  const R deltarh2 = deltarh * deltarh;
+  const R gamma = r * k.ov * s;                 // Eq. 24
+  const R gamma2 = gamma * gamma;
+  const R r2 = r * r;
+  const R inv_r = M::rcp(r);
+  const R inv_r2 = inv_r * inv_r;
+  const R rd2 = r2 * deltarh2;
+  const R Cb = R(1) + gamma2 + rd2;            // Eq. 26
+  const R inv_Cb = M::rcp(Cb);
+  const R sqCb = M::sqrt(Cb);
+  const R isqCb = M::rcp(sqCb);
+  const R Cb15 = Cb * sqCb;
+  const R inv_Cb15 = inv_Cb * isqCb;
+  const R inv_Cb25 = inv_Cb15 * inv_Cb;
+  const R inv_Cb2 = inv_Cb * inv_Cb;
+  const R inv_Cb3 = inv_Cb2 * inv_Cb;
+  const R Pc = (P < (R)0.1f) ? (R)0.1f : P;
+  const R Kpar = k.kpar_c * beta * Pc * r2 * isqCb;   // Eq. 32
+  const R Kper = k.ratio * Kpar;                        // Eq. 33
+  const R dKp = Kpar - Kper;
+  const R Krr = Kper + dKp * inv_Cb;                    // Eq. 27
+  const R Ktt = Kper + rd2 * dKp * inv_Cb;              // Eq. 28
+  const R Krt = deltarh * dKp * r * inv_Cb;             // Eq. 29
+  const R inv_Ktt = M::rcp(Ktt);
+  const R sq2Ktt = M::sqrt(R(2) * Ktt);
+  const R B11 = M::sqrt(R(2) * (Krr * Ktt - Krt * Krt) * inv_Ktt);   // Eq. 16
+  const R B12 = Krt * inv_Ktt * sq2Ktt;                              // Eq. 17
+  const R B22 = sq2Ktt * inv_r;                                      // Eq. 18
+  const R COmega = R(2) * r * k.ov2 * s * s + R(2) * r * deltarh2;   // Eq. 34
+  const R KbR = k.K0 * beta * P;
+  const R kd = k.kd_c * beta * P;                                    // K0 beta P / (3 * 5/3.4)
+  const R dKper = k.ratio * kd * (R(2) * r * sqCb - r2 * COmega * R(0.5) * isqCb) * inv_Cb;   // Eq. 36
+  const R dKrr = dKper + k.one_m_ratio * kd * (R(2) * r * Cb15 - R(1.5) * r2 * COmega * sqCb) * inv_Cb3;  // Eq. 35
+  const R CKtt0 = s * c * k.ov2 * r2;                                // Eq. 37
+  R dKtt, dKrtt;
+  const R base = k.one_m_ratio * kd * r2 * r * inv_rh * inv_Cb25;    // Eq. 44 prefactor
+  if (nonpolarB) {
+    const R dKtt1 = -k.ratio * kd * r2 * CKtt0 * inv_Cb15;           // Eq. 38
+    const R dKtt2 = k.one_m_ratio * KbR * r2 * r2 * deltarh2;         // Eq. 39
+    const R dKtt4 = R(3) * CKtt0 * inv_Cb25;                           // Eq. 41
+    dKtt = dKtt1 - dKtt2 * dKtt4;                                      // Eq. 42
+    dKrtt = -base * delta * R(3) * gamma2 * c * inv_s;
+  } else {
+    const R inv_s2 = inv_s * inv_s;
+    const R inv_s3 = inv_s2 * inv_s;
+    const R CKtt = CKtt0 - r2 * k.d0rh2 * c * inv_s3;
+    const R dKtt1 = -k.ratio * kd * r2 * CKtt * inv_Cb15;
+    const R dKtt2 = k.one_m_ratio * KbR * r2 * r2 * k.d0rh2;
+    const R dKtt3 = R(-2) * c * inv_s3 * k.inv_3c53 * inv_Cb15;              // Eq. 40
+    const R dKtt4 = R(3) * CKtt * inv_s2 * k.inv_3c53 * inv_Cb25;
+    dKtt = dKtt1 + dKtt2 * (dKtt3 - dKtt4);
+    dKrtt = -base * k.delta0 * c * inv_s2 * (R(1) - R(2) * rd2 + R(4) * gamma2);
+  }
+  const R dKrtr = k.one_m_ratio * kd * deltarh * r2 * inv_Cb25;      // Eq. 43
+  const R dt = k.dt;
+  R dr = (-k.V + R(2) * Krr * inv_r + dKrr) * dt;                     // Eq. 21
+  dr += dKrtt * dt * inv_r + Krt * c * dt * inv_r * inv_s;
+  dr += (n1 * B11 + n2 * B12) * k.sqdt;
+  R dth = Ktt * c * inv_r2 * inv_s * dt + dKtt * dt * inv_r2;         // Eq. 22
+  dth += dKrtr * dt + R(2) * Krt * dt * inv_r;
+  dth += n4 * B22 * k.sqdt;
+  const R dT = -k.adv * T2 * inv_Tp * T * inv_r;                      // Eq. 23
+  // Wavy current sheet drifts, Kappl 2016 Eq. 26 and 32-37.
+  const R Larmor = R(0.0225) * P * r2 * isqCb * M::rcp((R)kA);         // 0.0225 P / (A sqrt(Cb) / r^2)
+  const R xarg = k.alphaM + R(2) * (R)kPi * M::rcp(R(180)) * Larmor * inv_r;
+  const R q = M::div((R)kPi, M::sin(xarg)) - R(1);
+  const R ca = M::rcp(q);
+  const R alphaH = M::acos(ca);
+  const R tanH = M::sqrt(R(1) - ca * ca) * q;                          // tan(acos(ca))
+  const R inv_alphaH = M::rcp(alphaH);
+  const R arg = (R(1) - R(2) * th * M::rcp((R)kPi)) * tanH;
+  const R f = M::atan(arg) * inv_alphaH;
+  const R dc = k.drift2 * P * beta * r * gamma * f * inv_Cb2;
+  const R DriftR = dc * c * inv_s;
+  const R DriftTheta = -dc * (R(2) + gamma2);
+  const R fprime = -tanH * M::rcp(R(1) + arg * arg) * R(2) * M::rcp((R)kPi) * inv_alphaH;
+  const R DriftSheetR = k.drift1 * P * beta * r * gamma * fprime * inv_Cb;
+  dr += (DriftR + DriftSheetR) * dt;
+  dth += DriftTheta * dt * inv_r;
+  L.r.add(dr);
+  L.th.add(dth);
+  L.T.add(-dT);
+  if (L.th.v < R(0)) L.th.negate();
+  if (L.th.v > (R)kTwoPi) { L.th.set(L.th.v - (R)kTwoPi); }
+  else if (L.th.v > (R)kPi) { L.th.set((R)kTwoPi - L.th.v); }
+  if (L.r.v < R(0)) L.r.negate();
+  if (L.r.v > R(100)) return kRecordAndStop;
+  return (L.r.v < R(100)) ? kContinue : kStop;   // NaN or r == 100 end the reference loop
+}
+
+// ---------------------------------------------------------------------------
+// 2D SolarProp-like: SolarPropLikeModel.cu:95-247 (Kappl 2016 Eq. 13-18, 26,
+// 32-37, 42-44).
+// ---------------------------------------------------------------------------
+template <class R>
+__device__ __forceinline__ int step_solarprop(Lane<R> &L, const Consts<R> &k, R z0, R z1) {
+  using M = Math<R>;
+  const R r = L.r.v, th = L.th.v, T = L.T.v;
+  const R T0 = (R)kT0;
+  R s, c;
+  M::sincos(th, &s, &c);
+  const R inv_s = M::rcp(s);
+  const R gamma = r * k.ov * s;
+  const R gamma2 = gamma * gamma;
+  const R Tp = T + T0;
+  const R P = M::sqrt(T * (Tp + T0));
+  const R beta = P * M::rcp(Tp);
+  const R g1 = R(1) + gamma2;
+  const R inv_g1 = M::rcp(g1);
+  const R sq1 = M::sqrt(g1);
+  const R isq1 = M::rcp(sq1);
+  const R r2 = r * r;
+  const R inv_r = M::rcp(r);
+  const R tmp = R(2) * r * k.ov2 * s * s;                                       // Eq. 44
+  const R kbr = k.K0 * beta * P;
+  R dKrr = k.ratio * kbr * (R(2) * r * sq1 - r2 * tmp * R(0.5) * isq1) * inv_g1;
+  dKrr += k.one_m_ratio * kbr * (R(2) * r * g1 * sq1 - R(1.5) * r2 * tmp * sq1) * inv_g1 * inv_g1 * inv_g1;
+  dKrr = dKrr * R(5) * M::rcp(R(3) * (R)3.4f);
+  const R Pc = (P < (R)0.1f) ? (R)0.1f : P;
+  const R Kpar = k.kpar_c * beta * Pc * r2 * isq1;                              // Eq. 42
+  const R Kper = k.ratio * Kpar;                                                // Eq. 43
+  const R Krr = Kper + (Kpar - Kper) * inv_g1;                                  // Eq. 14
+  const R dt = k.dt;
+  R dr = (-k.V + R(2) * Krr * inv_r + dKrr) * dt + z0 * M::sqrt(R(2) * Krr * dt);   // Eq. 16
+  const R Ktt = Kper;                                                           // Eq. 15
+  R dth = Ktt * c * inv_r * inv_r * inv_s * dt * inv_g1;                        // Eq. 17
+  dth += z1 * M::sqrt(R(2) * Ktt * dt) * inv_r;
+  const R dT = -k.adv * (Tp + T0) * M::rcp(Tp) * T * inv_r;                    // Eq. 18
+  const R Larmor = R(0.0225) * P * r2 * isq1 * M::rcp((R)kA);
+  const R xarg = k.alphaM + R(2) * (R)kPi * M::rcp(R(180)) * Larmor * inv_r;
+  const R q = M::div((R)kPi, M::sin(xarg)) - R(1);
+  const R ca = M::rcp(q);
+  const R alphaH = M::acos(ca);
+  const R tanH = M::sqrt(R(1) - ca * ca) * q;
+  const R inv_alphaH = M::rcp(alphaH);
+  const R arg = (R(1) - R(2) * th * M::rcp((R)kPi)) * tanH;
+  const R f = M::atan(arg) * inv_alphaH;
+  const R fprime = -tanH * M::rcp(R(1) + arg * arg) * R(2) * M::rcp((R)kPi) * inv_alphaH;
+  const R inv_g1sq = inv_g1 * inv_g1;
+  const R pbr = P * beta * r * gamma;
+  const R DriftR = k.drift2 * pbr * c * f * inv_g1sq * inv_s;                  // Eq. 35
+  const R DriftSheetR = k.drift1 * pbr * fprime * inv_g1;                     // Eq. 37
+  dr += (DriftR + DriftSheetR) * dt;
+  const R DriftTheta = k.dtheta_sp * pbr * (R(2) + gamma2) * f * inv_g1sq;     // Eq. 36
+  dth += DriftTheta * dt * inv_r;
+  L.r.add(dr);
+  L.th.add(dth);
+  L.T.add(-dT);
+  if (L.th.v < R(0)) L.th.negate();
+  if (L.th.v > (R)kTwoPi) { L.th.set(L.th.v - (R)kTwoPi); }
+  else if (L.th.v > (R)kPi) { L.th.set((R)kTwoPi - L.th.v); }
+  if (L.r.v < R(0)) L.r.negate();
+  if (L.r.v > R(100)) return kRecordAndStop;
+  return (L.r.v < R(100)) ? kContinue : kStop;
+}
+
+// Kinetic energy [GeV] from rigidity [GV] without cancellation.
+template <class R>
+__device__ __forceinline__ R kinetic_from_rigidity(R P) {
+  const R T0 = (R)kT0;
+  return P * P * Math<R>::rcp(Math<R>::sqrt(T0 * T0 + P * P) + T0);
+}
+
+// ---------------------------------------------------------------------------
+// 1D B-p: OneDimensionBpModel.cu:69-140 (Eq. 5-7, 12-14).  V < 0.
+// ---------------------------------------------------------------------------
+template <class R>
+__device__ __forceinline__ int step_bp(Lane<R> &L, const Consts<R> &k, R z) {
+  using M = Math<R>;
+  const R r = L.r.v, T = L.T.v;
+  const R T0 = (R)kT0;
+  const R beta0 = M::sqrt(T * (T + T0 + T0)) * M::rcp(T + T0);
+  const R Rig = L.P.v;
+  const Acc<R> Psave = L.P;
+  const Acc<R> rsave = L.r;
+  const R inv_r = M::rcp(r);
+  L.P.add(-k.adv * Rig * inv_r);                        // Eq. 14
+  const R Kdiff = k.K0 * beta0 * Rig;                   // Eq. 7
+  const R dr = (k.V + R(2) * Kdiff * inv_r) * k.dt + z * M::sqrt(R(2) * Kdiff * k.dt);   // Eq. 13
+  L.r.add(dr);
+  const R Tn = kinetic_from_rigidity(L.P.v);
+  L.T.set(Tn);
+  const R beta = M::sqrt(Tn * (Tn + T0 + T0)) * M::rcp(Tn + T0);
+  const R rn = L.r.v;
+  if (beta > (R)0.01f && Tn < R(200)) {
+    if (rn > R(100) && (rn - dr) < R(100)) return kRecordAndStop;
+  } else if (beta < (R)0.01f) {
+    return kStop;
+  }
+  if (rn < (R)0.3f) {           // reflecting inner boundary: undo r and p; T keeps
+    L.r = rsave;                 // the rejected step's value, as in the reference
+    L.P = Psave;
+  }
+  return (L.r.v < (R)100.0002f) ? kContinue : kStop;
+}
+
+// ---------------------------------------------------------------------------
+// 1D F-p: OneDimensionFpModel.cu:73-141 (Eq. 5-11).  Records every 1 AU crossing.
+// ---------------------------------------------------------------------------
+template <class R>
+__device__ __forceinline__ int step_fp(Lane<R> &L, const Consts<R> &k, R z) {
+  using M = Math<R>;
+  const R r = L.r.v, T = L.T.v;
+  const R T0 = (R)kT0;
+  const R P0 = M::sqrt(T * (T + T0 + T0));
+  const R beta = P0 * M::rcp(T + T0);
+  const R inv_r = M::rcp(r);
+  L.sumac.add(R(2) * k.adv * inv_r);                    // Eq. 11: 4 V dt / (3 r)
+  const Acc<R> Psave = L.P;
+  const Acc<R> rsave = L.r;
+  L.P.add(-k.adv * L.P.v * inv_r);                      // Eq. 10
+  const R Kdiff = k.K0 * beta * P0;                     // Eq. 7
+  const R dr = (k.V + R(2) * Kdiff * inv_r) * k.dt + z * M::sqrt(R(2) * Kdiff * k.dt);   // Eq. 9
+  L.r.add(dr);
+  const R Tn = kinetic_from_rigidity(L.P.v);
+  L.T.set(Tn);
+  const R rn = L.r.v;
+  int res = kContinue;
+  if (beta > (R)0.01f && Tn < R(100)) {
+    if ((rn - R(1)) / ((rn - dr) - R(1)) < R(0)) res = kRecordAndContinue;
+  } else if (beta < (R)0.01f) {
+    return kStop;
+  }
+  if (rn < (R)0.1f) {           // undo r and p (T keeps the rejected step's value)
+    L.r = rsave;
+    L.P = Psave;
+  }
+  if (!(L.r.v < (R)100.0002f)) return (res == kRecordAndContinue) ? kRecordAndStop : kStop;
+  return res;
+}
+
+}  // namespace gelio

@@ -1,0 +1,165 @@
+"""Spectrum-level parity of the fused GPU path.
+
+* against the reference CPU models (statistical: per-bin means within MC
+  error, tests/golden/ref_spectra_*.json made from the reference itself);
+* against the reference evaluation of the GPU's own exit records printed to
+  log.dat (deterministic: identical bins and counts);
+* internal consistency: batched vs single, persistent vs plain, graph vs
+  stream, repeatability.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from geliosphere_gb300 import abi, make_sim, spectra_dict
+from geliosphere_gb300.engine import records_to_log_rows, round_g, deg_rad
+
+pytestmark = pytest.mark.gpu
+
+
+def sim_from_fixture(doc, n, seed):
+    """gelio_sim_params with the resolved statics the reference run used."""
+    r = doc["resolved"]
+    model = {"fp": 0, "bp": 1, "solarprop": 2, "geliosphere": 3}[doc["model"]]
+    p = make_sim(model, n, seed=seed)
+    p.K0 = r["K0"]
+    p.V = abs(r["V"])
+    p.dt = r["dt"]
+    p.r_injection = r["rInit"]
+    p.theta_injection = r["thetainj"]
+    p.tilt = r["alphaM"]
+    p.polarity = r["polarity"]
+    p.ratio = r["ratio"]
+    p.delta0 = r["delta0"]
+    p.injection_max = r["uniformEnergyInjectionMaximum"]
+    if model >= 2:
+        p.injection = abi.GELIO_INJ_SOLARPROP_GRID
+        # the CPU model uses the polarity in the SolarProp theta drift
+        p.flags = abi.GELIO_FLAG_SOLARPROP_THETA_DRIFT_POLARITY
+    else:
+        p.injection = abi.GELIO_INJ_CPU_UNIFORM
+    return p
+
+
+def mean_and_err(w, w2, n):
+    n = np.asarray(n, dtype=np.float64)
+    m = np.where(n > 0, w / np.maximum(n, 1), 0.0)
+    var = np.where(n > 1, (w2 / np.maximum(n, 1) - m * m) / np.maximum(n - 1, 1), np.inf)
+    return m, np.sqrt(np.maximum(var, 0))
+
+
+def compare_sections(gpu, ref, sections, min_count=200):
+    zs = []
+    for wkey, w2key, nkey in sections:
+        mg, eg = mean_and_err(np.array(gpu[wkey]), np.array(gpu[w2key]), np.array(gpu[nkey]))
+        mr, er = mean_and_err(np.array(ref[wkey]), np.array(ref[w2key]), np.array(ref[nkey]))
+        ok = (np.array(gpu[nkey]) >= min_count) & (np.array(ref[nkey]) >= min_count)
+        z = (mg[ok] - mr[ok]) / np.sqrt(eg[ok] ** 2 + er[ok] ** 2)
+        zs.append(z)
+    return np.concatenate(zs)
+
+
+@pytest.mark.parametrize("case", ["geliosphere_a_pos_tilt20", "geliosphere_a_neg_tilt70", "solarprop_a_pos"])
+def test_2d_spectra_match_reference_cpu_model(engine, case):
+    path = os.path.join(GOLDEN, f"ref_spectra_{case}.json")
+    if not os.path.exists(path):
+        pytest.skip("fixture not generated")
+    doc = json.load(open(path))
+    sim = sim_from_fixture(doc, 3_000_000, seed=2024)
+    gpu = spectra_dict(engine.run(sim).spectra[0])
+    ref = doc["spectra"]
+    z = compare_sections(gpu, ref, [("sp_weber", "sp_weber2", "sp_n"), ("sp_jgr", "sp_jgr2", "sp_n"),
+                                    ("sp_burger", "sp_burger2", "sp_n")])
+    assert z.size >= 60
+    # per-bin mean weights within Monte Carlo error (the three LIS share particles)
+    zb = z[: z.size // 3]
+    chi2_dof = float(np.mean(zb ** 2))
+    print(f"{case}: bins {zb.size}, max|z| {np.abs(z).max():.2f}, chi2/dof {chi2_dof:.3f}, "
+          f"within 3 sigma {np.mean(np.abs(z) < 3):.3f}")
+    assert np.abs(z).max() < 4.0
+    assert chi2_dof < 1.6
+
+
+def test_bp_spectra_match_reference_cpu_model(engine):
+    path = os.path.join(GOLDEN, "ref_spectra_bp_dt50.json")
+    if not os.path.exists(path):
+        pytest.skip("fixture not generated")
+    doc = json.load(open(path))
+    sim = sim_from_fixture(doc, 2_000_000, seed=77)
+    gpu = spectra_dict(engine.run(sim).spectra[0])
+    z = compare_sections(gpu, doc["spectra"], [("e2_w", "e2_w2", "e2_n")], min_count=100)
+    print(f"bp: bins {z.size}, max|z| {np.abs(z).max():.2f}, chi2/dof {np.mean(z**2):.3f}")
+    assert z.size >= 50
+    assert np.abs(z).max() < 4.0
+    assert np.mean(z ** 2) < 1.6
+
+
+@pytest.mark.parametrize("model", [abi.GELIO_MODEL_2D_GELIOSPHERE, abi.GELIO_MODEL_2D_SOLARPROP,
+                                   abi.GELIO_MODEL_1D_BP, abi.GELIO_MODEL_1D_FP])
+def test_fused_evaluation_equals_reference_text_pipeline(engine, oracle, model):
+    """Binning in the kernel == printing the same records to log.dat and
+    running the reference evaluator on it."""
+    if model == abi.GELIO_MODEL_1D_FP:
+        sim = make_sim(model, 400_000, dt=50, seed=5, injection=abi.GELIO_INJ_REFERENCE_UNIFORM)
+    elif model == abi.GELIO_MODEL_1D_BP:
+        sim = make_sim(model, 20_000, dt=50, seed=5)
+    else:
+        sim = make_sim(model, 60_000, dt=500, tilt_deg=20, seed=5, injection=abi.GELIO_INJ_REFERENCE_UNIFORM)
+    res = engine.run(sim, record_capacity=2_000_000)
+    gpu = spectra_dict(res.spectra[0])
+    recs = res.records
+    assert res.stats.n_records_dropped == 0 and len(recs) == int(gpu["n_records"])
+    rows = round_g(records_to_log_rows(model, recs, sim.theta_injection))
+    ref = spectra_dict(oracle.evaluate(model, rows))
+    count_keys = ["sp_n", "uly_n", "ams_n"] if model >= 2 else ["e2_n", "e3_n", "e4_n", "log_n"]
+    val_keys = ["sp_weber", "sp_jgr", "sp_burger", "uly_w", "ams_w"] if model >= 2 else \
+        ["e2_w", "e3_w", "e4_w", "log_w"]
+    for k in count_keys:
+        np.testing.assert_array_equal(gpu[k], ref[k], err_msg=k)
+    for k in val_keys:
+        np.testing.assert_allclose(gpu[k], ref[k], rtol=1e-11, atol=0, err_msg=k)
+
+
+def test_batch_equals_single_runs(engine):
+    sims = [make_sim(abi.GELIO_MODEL_2D_GELIOSPHERE, 30_000, tilt_deg=t, polarity=p, seed=100 + i,
+                     injection=abi.GELIO_INJ_LOG_GRID, inj_points=50)
+            for i, (t, p) in enumerate([(10, 1), (45, -1), (70, 1)])]
+    sims.append(make_sim(abi.GELIO_MODEL_1D_BP, 5_000, seed=9))
+    batch = [spectra_dict(s) for s in engine.run(sims).spectra]
+    for i, s in enumerate(sims):
+        single = spectra_dict(engine.run(s).spectra[0])
+        for k in ("sp_n", "ams_n", "grid_n", "e2_n", "n_particles", "n_records", "n_steps"):
+            np.testing.assert_array_equal(batch[i][k], single[k], err_msg=f"sim {i} {k}")
+        for k in ("sp_burger", "grid_w", "e2_w"):
+            np.testing.assert_allclose(batch[i][k], single[k], rtol=1e-12, err_msg=f"sim {i} {k}")
+
+
+def test_persistent_plain_graph_and_repeat_agree(engine):
+    sim = make_sim(abi.GELIO_MODEL_2D_GELIOSPHERE, 50_000, tilt_deg=20, seed=3,
+                   injection=abi.GELIO_INJ_LOG_GRID, inj_points=100)
+    a = spectra_dict(engine.run(sim).spectra[0])
+    b = spectra_dict(engine.run(sim, plain=True).spectra[0])
+    c = spectra_dict(engine.run(sim, use_graph=True).spectra[0])
+    d = spectra_dict(engine.run(sim, use_graph=True).spectra[0])
+    e = spectra_dict(engine.run(sim, refill=8, block_size=128).spectra[0])
+    for other in (b, c, d, e):
+        for k in ("grid_n", "sp_n", "n_records", "n_steps", "n_lost"):
+            np.testing.assert_array_equal(a[k], other[k], err_msg=k)
+        np.testing.assert_allclose(a["grid_w"], other["grid_w"], rtol=1e-12)
+    assert a["n_particles"] == 50_000
+
+
+def test_fp32_and_fp64_runs_agree(engine):
+    sim = make_sim(abi.GELIO_MODEL_1D_BP, 20_000, dt=50, seed=8, injection=abi.GELIO_INJ_LOG_GRID,
+                   inj_points=40, inj_min=0.05, inj_max=50.0)
+    a = spectra_dict(engine.run(sim).spectra[0])
+    b = spectra_dict(engine.run(sim, precision=abi.GELIO_PREC_FP64).spectra[0])
+    # same random stream: all but a handful of trajectories end identically
+    assert abs(a["n_records"] - b["n_records"]) <= 0.002 * b["n_records"]
+    ok = b["grid_n"] > 100
+    rel = np.abs(a["grid_w"][0][ok] / a["grid_n"][ok] - b["grid_w"][0][ok] / b["grid_n"][ok]) / \
+        (b["grid_w"][0][ok] / b["grid_n"][ok])
+    assert rel.max() < 2e-3

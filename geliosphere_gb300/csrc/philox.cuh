@@ -50,10 +50,11 @@ __host__ __device__ __forceinline__ Philox4 philox4x32_10(Philox4 c, uint32_t k0
   return c;
 }
 
-// 24-bit uniform in (0, 1): (x >> 8) * 2^-24 + 2^-25.  Exact in FP32 (and
-// therefore identical in the FP64 oracle); never 0, so log() is finite.
-__host__ __device__ __forceinline__ float u32_to_unit(uint32_t x) {
-  return (float)(x >> 8) * 5.9604644775390625e-8f + 2.98023223876953125e-8f;
+// 23-bit uniform in (0, 1): (x >> 9) * 2^-23 + 2^-24 = (2 (x >> 9) + 1) 2^-24,
+// an odd multiple of 2^-24 below 1, so exactly representable in FP32 (and
+// identical in the FP64 oracle); never 0, so log() is finite.
+__device__ __forceinline__ float u32_to_unit(uint32_t x) {
+  return __uint2float_rn(2u * (x >> 9) + 1u) * 5.9604644775390625e-8f;
 }
 
 // Box-Muller: z0 = sqrt(-2 ln u1) cos(2 pi u2), z1 = sqrt(-2 ln u1) sin(2 pi u2).

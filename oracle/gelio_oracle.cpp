@@ -65,8 +65,8 @@ void philox(const uint32_t in[4], const uint32_t key[2], uint32_t out[4]) {
   out[0] = x0; out[1] = x1; out[2] = x2; out[3] = x3;
 }
 
-double unit24(uint32_t x) {   // exact float value (x >> 8) 2^-24 + 2^-25
-  return (double)(x >> 8) * (1.0 / 16777216.0) + (1.0 / 33554432.0);
+double unit24(uint32_t x) {   // the engine's uniform (2 (x >> 9) + 1) 2^-24, exact
+  return (double)(2u * (x >> 9) + 1u) * (1.0 / 16777216.0);
 }
 
 // The engine's four normals for counter word `ctr0` of a trajectory.

@@ -130,7 +130,7 @@ PROTOTYPES = {
                             POINTER(Spectra), POINTER(RunStats)]),
     "gelio_run_async": (c_int32, [c_void_p, c_void_p, c_int32, POINTER(RunOpts), c_void_p, c_void_p]),
     "gelio_last_stats": (c_int32, [c_void_p, POINTER(RunStats)]),
-    "gelio_replay": (c_int32, [c_void_p, POINTER(SimParams), c_int64, c_int64, c_int32,
+    "gelio_replay": (c_int32, [c_void_p, POINTER(SimParams), c_int64, c_int64, c_int32, c_uint64,
                                POINTER(Trajectory)]),
     "gelio_evaluate": (c_int32, [c_void_p, c_int32, POINTER(c_double), c_int64, c_int32,
                                  POINTER(Spectra)]),

@@ -724,7 +724,7 @@ int32_t gelio_last_stats(gelio_ctx *c, gelio_run_stats *stats) {
 }
 
 int32_t gelio_replay(gelio_ctx *c, const gelio_sim_params *sim, int64_t first, int64_t count,
-                     int32_t precision, gelio_trajectory *out) {
+                     int32_t precision, uint64_t max_steps, gelio_trajectory *out) {
   if (!c || !sim || first < 0 || count < 0 || (count > 0 && !out)) return GELIO_ERR_INVALID_ARGUMENT;
   if (precision != GELIO_PREC_FP32 && precision != GELIO_PREC_FP64) return GELIO_ERR_INVALID_ARGUMENT;
   int rc = validate_params(*sim);
@@ -753,7 +753,7 @@ int32_t gelio_replay(gelio_ctx *c, const gelio_sim_params *sim, int64_t first, i
   a.n_slices = 1;
   a.part = c->d_part;
   a.ctl = c->d_ctl;
-  a.max_steps = 100000000ull;
+  a.max_steps = (max_steps > 0 && max_steps < 0xfffffff0ull) ? max_steps : 100000000ull;
   a.plain_sim = 0;
   a.plain_first = (unsigned long long)first;
   a.plain_count = (unsigned long long)count;

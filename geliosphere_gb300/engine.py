@@ -186,9 +186,11 @@ class Engine:
         abi.check(self.lib.gelio_last_stats(self.ctx, byref(s)), "gelio_last_stats")
         return s
 
-    def replay(self, sim: abi.SimParams, first: int, count: int, precision: int = 0) -> np.ndarray:
+    def replay(self, sim: abi.SimParams, first: int, count: int, precision: int = 0,
+               max_steps: int = 0) -> np.ndarray:
         buf = (abi.Trajectory * max(count, 1))()
-        abi.check(self.lib.gelio_replay(self.ctx, byref(sim), first, count, precision, buf), "gelio_replay")
+        abi.check(self.lib.gelio_replay(self.ctx, byref(sim), first, count, precision, max_steps, buf),
+                  "gelio_replay")
         return np.frombuffer(bytes(buf)[: count * TRAJ_DTYPE.itemsize], dtype=TRAJ_DTYPE).copy()
 
     def evaluate(self, model: int, rows: np.ndarray) -> abi.Spectra:

@@ -264,10 +264,12 @@ int32_t gelio_run_async(gelio_ctx *ctx, const gelio_sim_params *d_sims,
 int32_t gelio_last_stats(gelio_ctx *ctx, gelio_run_stats *stats);
 
 /* Per-trajectory exit states of particles [first, first + count) of one
- * simulation, in the requested precision (host output, count entries). */
+ * simulation, in the requested precision (host output, count entries).
+ * max_steps > 0 stops every trajectory after that many steps (status 2), so
+ * states can be compared at a fixed step; 0 = 100,000,000. */
 int32_t gelio_replay(gelio_ctx *ctx, const gelio_sim_params *sim,
                      int64_t first, int64_t count, int32_t precision,
-                     gelio_trajectory *out);
+                     uint64_t max_steps, gelio_trajectory *out);
 
 /* Bin existing log.dat rows on the device, as the evaluators do.  rows is
  * row-major [n_rows][n_cols] host doubles in the column order of the

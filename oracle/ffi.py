@@ -95,7 +95,7 @@ def injection(sim: abi.SimParams, pid: int) -> float:
     return float(load().gor_injection(ctypes.byref(sim), pid))
 
 
-def replay(sim: abi.SimParams, first: int, count: int, max_steps: int = 0):  # noqa: D401
+def replay(sim: abi.SimParams, first: int, count: int, max_steps: int = 0):
     """GPU-flavour FP64 replay: (status, steps, nrec, values[count, 6]) with
     values = T_final, r_final, aux_final, T_record, r_record, aux_record."""
     lib = load()

@@ -231,7 +231,9 @@ def main():
     d_sims = torch.frombuffer(bytearray(raw), dtype=torch.uint8).to(f"cuda:{local}")
     d_out = torch.zeros(n * ctypes.sizeof(abi.Spectra), dtype=torch.uint8, device=f"cuda:{local}")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the kernels and the timing events share it
+    stream = torch.cuda.Stream(device=local)
+    torch.cuda.set_stream(stream)
 
     def one_step():
         st = eng.run_async(d_sims.data_ptr(), n, d_out.data_ptr(), stream.cuda_stream)

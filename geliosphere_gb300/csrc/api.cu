@@ -324,6 +324,8 @@ struct gelio_ctx {
   // pinned staging
   gelio_sim_params *h_params = nullptr;
   int h_params_cap = 0;
+  gelio_spectra *h_out = nullptr;      // pinned staging of graph-mode outputs
+  int h_out_cap = 0;
   Control *h_ctl = nullptr;
   // graph cache
   cudaGraphExec_t graph = nullptr;
@@ -367,6 +369,7 @@ static void release(gelio_ctx *c) {
   cudaFree(c->d_gpre); cudaFree(c->d_ctl); cudaFree(c->d_part); cudaFree(c->d_out);
   cudaFree(c->d_rec); cudaFree(c->d_traj); cudaFree(c->d_rows);
   if (c->h_params) cudaFreeHost(c->h_params);
+  if (c->h_out) cudaFreeHost(c->h_out);
   if (c->h_ctl) cudaFreeHost(c->h_ctl);
   if (c->ev_k0) cudaEventDestroy(c->ev_k0);
   if (c->ev_k1) cudaEventDestroy(c->ev_k1);
@@ -630,8 +633,18 @@ int32_t gelio_run(gelio_ctx *c, const gelio_sim_params *sims, int32_t n, const g
     (unsigned long long)(o ? o->refill_interval : 0), (unsigned long long)rec_cap,
     (unsigned long long)(o ? o->max_steps_per_particle : 0),
     (unsigned long long)((o ? o->time_limit_s : 0.0) * 1e9)};
+  if (graph && n > c->h_out_cap) {
+    if (c->h_out) cudaFreeHost(c->h_out);
+    c->h_out = nullptr;
+    c->h_out_cap = 0;
+    if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+    GELIO_TRY(cudaMallocHost(&c->h_out, sizeof(gelio_spectra) * c->cap_sims));
+    c->h_out_cap = c->cap_sims;
+  }
   if (graph) {
-    const bool hit = c->graph && memcmp(key, c->graph_key, sizeof(key)) == 0 && c->graph_out == out;
+    // graphs copy through pinned staging (pageable host memory cannot be a
+    // memcpy node); the staging pointer is fixed, so the graph is reusable
+    const bool hit = c->graph && memcmp(key, c->graph_key, sizeof(key)) == 0 && c->graph_out == c->h_out;
     if (!hit) {
       if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
       cudaGraph_t gr;
@@ -641,7 +654,7 @@ int32_t gelio_run(gelio_ctx *c, const gelio_sim_params *sims, int32_t n, const g
       int erc = (e == cudaSuccess) ? enqueue_run(c, n, o, c->d_out, st, mask, counts, rec_cap ? c->d_rec : nullptr, rec_cap, true)
                                    : map_cuda(e);
       if (erc == GELIO_OK) {
-        e = cudaMemcpyAsync(out, c->d_out, sizeof(gelio_spectra) * n, cudaMemcpyDeviceToHost, st);
+        e = cudaMemcpyAsync(c->h_out, c->d_out, sizeof(gelio_spectra) * n, cudaMemcpyDeviceToHost, st);
         if (e != cudaSuccess) erc = map_cuda(e);
       }
       cudaError_t ee = cudaStreamEndCapture(st, &gr);
@@ -651,7 +664,7 @@ int32_t gelio_run(gelio_ctx *c, const gelio_sim_params *sims, int32_t n, const g
       cudaGraphDestroy(gr);
       GELIO_TRY(e);
       memcpy(c->graph_key, key, sizeof(key));
-      c->graph_out = out;
+      c->graph_out = c->h_out;
     }
     GELIO_TRY(cudaGraphLaunch(c->graph, st));
   } else {
@@ -661,6 +674,7 @@ int32_t gelio_run(gelio_ctx *c, const gelio_sim_params *sims, int32_t n, const g
     GELIO_TRY(cudaMemcpyAsync(out, c->d_out, sizeof(gelio_spectra) * n, cudaMemcpyDeviceToHost, st));
   }
   GELIO_TRY(cudaStreamSynchronize(st));
+  if (graph) memcpy(out, c->h_out, sizeof(gelio_spectra) * n);
   const Control &h = *c->h_ctl;
   if (h.status != 0) return (int)h.status;
   int64_t stored = 0;

@@ -136,6 +136,7 @@ __device__ __forceinline__ void init_lane(Lane<R> &L, Consts<R> &K, const SimDev
   L.Tinj = Tinj;
   L.T.set((R)Tinj);
   const R T0 = (R)kT0;
+  L.thn = 0.0f;
   if constexpr (MODEL == kModelGeliosphere || MODEL == kModelSolarProp) {
     L.r.set((R)sd.r_inj);
     L.th.set((R)sd.theta_inj);
@@ -462,7 +463,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4) ? 2 : 1) k_persistent(co
                   pd.Tinj = L.Tinj;
                   pd.Texit = (float)L.T.v;
                   pd.r = (float)L.r.v;
-                  pd.aux = (float)L.th.v;
+                  pd.aux = (float)theta_full(L);
                   pd.sim = L.sim;
                   pd.slot = slot;
                   pd.gbin = L.gbin;
@@ -531,7 +532,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4) ? 2 : 1) k_plain(const K
           if (nrec == 0) {
             t_rec = (float)L.T.v;
             r_rec = (float)L.r.v;
-            aux_rec = (MODEL == kModelFp) ? (float)L.sumac.v : (float)L.th.v;
+            aux_rec = (MODEL == kModelFp) ? (float)L.sumac.v : (float)theta_full(L);
           }
           ++nrec;
         }
@@ -543,7 +544,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4) ? 2 : 1) k_plain(const K
           if (res == kRecordAndStop) {
             pending = true;
             status = 0;
-            pd.Tinj = L.Tinj; pd.Texit = (float)L.T.v; pd.r = (float)L.r.v; pd.aux = (float)L.th.v;
+            pd.Tinj = L.Tinj; pd.Texit = (float)L.T.v; pd.r = (float)L.r.v; pd.aux = (float)theta_full(L);
             pd.sim = sim; pd.slot = 1 << 30; pd.gbin = L.gbin; pd.pid = L.pid;
           } else {
             status = 1;
@@ -571,7 +572,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4) ? 2 : 1) k_plain(const K
     t.t_injection = L.Tinj;
     t.t_final = (float)L.T.v;
     t.r_final = (float)L.r.v;
-    t.theta_final = (MODEL == kModelFp) ? (float)L.sumac.v : (float)L.th.v;
+    t.theta_final = (MODEL == kModelFp) ? (float)L.sumac.v : (float)theta_full(L);
     t.t_record = t_rec;
     t.r_record = r_rec;
     t.aux_record = aux_rec;

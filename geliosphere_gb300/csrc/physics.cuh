@@ -176,6 +176,7 @@ __device__ __forceinline__ float inj_solarprop(unsigned long long s, const float
 // ---------------------------------------------------------------------------
 template <class R> struct Lane {
   Acc<R> r, th, T, P, sumac;
+  float thn;           // FP32 2D models: theta = 2 pi thn + th once theta has left [0, 2 pi)
   float Tinj;
   uint32_t steps;
   int sim;
@@ -188,13 +189,88 @@ template <class R> struct Lane {
 enum StepResult : int { kContinue = 0, kRecordAndStop = 1, kStop = 2, kRecordAndContinue = 3 };
 
 // ---------------------------------------------------------------------------
+// Theta bookkeeping of the 2D models.
+//
+// The reference reflects theta once per step (GeliosphereModel.cu:366-377):
+//   theta < 0 -> |theta|;  theta > 2 pi -> theta - 2 pi;  else theta > pi -> 2 pi - theta.
+// Near the poles the drift terms (1/sin^3 theta) can throw theta far outside
+// [0, pi]; a single reflection does not bring it back, and such "runaway"
+// trajectories (about 16% of 2D exits) keep |theta| up to 1e20 and beyond.
+// In FP64 their sin/cos still see the phase of theta; a plain FP32 theta
+// loses it above 2^24 rad (it freezes and its sin/cos are quantised), which
+// shortens those trajectories by ~10% and biases the low-energy spectra.
+// The FP32 kernels therefore keep a runaway theta as 2 pi * thn + phase with
+// the phase in [0, 2 pi): the reference's reflections act exactly on that
+// value, sin/cos use the full-precision phase, and FP64's freezing of theta
+// (an update below half an FP64 ulp of |theta| leaves it unchanged) is
+// reproduced.  Trajectories whose theta stays in [0, 2 pi) never take this path.
+// ---------------------------------------------------------------------------
+constexpr float kTwoPiHi = 6.28318548202514648f;     // 2 pi = kTwoPiHi + kTwoPiLo
+constexpr float kTwoPiLo = -1.74845553e-7f;
+constexpr float kInvTwoPi = 0.159154943091895336f;
+
+template <class R>
+__device__ __forceinline__ R theta_full(const Lane<R> &L) {
+  if constexpr (sizeof(R) == 4) return fmaf(L.thn, kTwoPiHi, L.th.v);
+  else return L.th.v;
+}
+
+__device__ __forceinline__ void phase_normalise(Acc<float> &ph, float &n) {
+  float x = ph.v;
+  if (x >= 0.0f && x < kTwoPiHi) return;
+  const float k = floorf(x * kInvTwoPi);
+  x = fmaf(-k, kTwoPiHi, x);
+  x = fmaf(-k, kTwoPiLo, x);
+  n += k;
+  if (x < 0.0f) { x += kTwoPiHi; n -= 1.0f; }
+  if (x >= kTwoPiHi) { x -= kTwoPiHi; n += 1.0f; }
+  ph.set(x);
+}
+
+template <class R>
+__device__ __forceinline__ void theta_update(Lane<R> &L, R dth) {
+  if constexpr (sizeof(R) == 8) {
+    L.th.add(dth);
+    if (L.th.v < R(0)) L.th.negate();
+    if (L.th.v > (R)kTwoPi) { L.th.set(L.th.v - (R)kTwoPi); }
+    else if (L.th.v > (R)kPi) { L.th.set((R)kTwoPi - L.th.v); }
+  } else {
+    if (L.thn == 0.0f) {
+      L.th.add(dth);
+      if (L.th.v < 0.0f) L.th.negate();
+      if (L.th.v > kTwoPi) { L.th.set(L.th.v - kTwoPi); }
+      else if (L.th.v > kPi) { L.th.set(kTwoPi - L.th.v); }
+      if (L.th.v >= kTwoPiHi) phase_normalise(L.th, L.thn);   // runaway: switch representation
+    } else {
+      // an update below half an FP64 ulp of |theta| leaves theta unchanged
+      if (fabsf(dth) < fabsf(L.thn) * kTwoPiHi * 1.1102230246251565e-16f) dth = 0.0f;
+      L.th.add(dth);
+      phase_normalise(L.th, L.thn);
+      if (L.thn < 0.0f) {                       // theta < 0 -> |theta|
+        L.thn = -L.thn - 1.0f;
+        L.th.set(kTwoPiHi - L.th.v);
+        phase_normalise(L.th, L.thn);
+      }
+      if (L.thn >= 1.0f && !(L.thn == 1.0f && L.th.v == 0.0f)) {
+        L.thn -= 1.0f;                          // theta > 2 pi -> theta - 2 pi
+      } else if (L.thn == 0.0f && L.th.v > kPi) {
+        L.th.set(kTwoPi - L.th.v);              // theta > pi -> 2 pi - theta
+      } else if (L.thn == 1.0f && L.th.v == 0.0f) {
+        L.thn = 0.0f;                           // theta == 2 pi -> 0
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // 2D Geliosphere: GeliosphereModel.cu:82-390 (Eq. 16-44 of the Geliosphere
 // model description, drifts of Kappl 2016 Eq. 26-37).
 // ---------------------------------------------------------------------------
 template <class R>
 __device__ __forceinline__ int step_geliosphere(Lane<R> &L, const Consts<R> &k, R n1, R n2, R n4) {
   using M = Math<R>;
-  const R r = L.r.v, th = L.th.v, T = L.T.v;
+  const R r = L.r.v, ph = L.th.v, T = L.T.v;
+  const R th = theta_full(L);
   const R T0 = (R)kT0;
   const R Tp = T + T0;
   const R T2 = Tp + T0;
@@ -202,7 +278,7 @@ __device__ __forceinline__ int step_geliosphere(Lane<R> &L, const Consts<R> &k, 
   const R inv_Tp = M::rcp(Tp);
   const R beta = P * inv_Tp;
   R s, c;
-  M::sincos(th, &s, &c);
+  M::sincos(ph, &s, &c);
   const R inv_s = M::rcp(s);
   const bool polarA = (th < (R)kThetaLo) || (th > (R)kThetaHi);   // Eq. 25 branch
   const bool nonpolarB = (th > (R)kThetaLo) && (th < (R)kThetaHi);
@@ -289,11 +365,8 @@ __device__ __forceinline__ int step_geliosphere(Lane<R> &L, const Consts<R> &k, 
   dr += (DriftR + DriftSheetR) * dt;
   dth += DriftTheta * dt * inv_r;
   L.r.add(dr);
-  L.th.add(dth);
+  theta_update(L, dth);
   L.T.add(-dT);
-  if (L.th.v < R(0)) L.th.negate();
-  if (L.th.v > (R)kTwoPi) { L.th.set(L.th.v - (R)kTwoPi); }
-  else if (L.th.v > (R)kPi) { L.th.set((R)kTwoPi - L.th.v); }
   if (L.r.v < R(0)) L.r.negate();
   if (L.r.v > R(100)) return kRecordAndStop;
   return (L.r.v < R(100)) ? kContinue : kStop;   // NaN or r == 100 end the reference loop
@@ -306,10 +379,11 @@ __device__ __forceinline__ int step_geliosphere(Lane<R> &L, const Consts<R> &k, 
 template <class R>
 __device__ __forceinline__ int step_solarprop(Lane<R> &L, const Consts<R> &k, R z0, R z1) {
   using M = Math<R>;
-  const R r = L.r.v, th = L.th.v, T = L.T.v;
+  const R r = L.r.v, ph = L.th.v, T = L.T.v;
+  const R th = theta_full(L);
   const R T0 = (R)kT0;
   R s, c;
-  M::sincos(th, &s, &c);
+  M::sincos(ph, &s, &c);
   const R inv_s = M::rcp(s);
   const R gamma = r * k.ov * s;
   const R gamma2 = gamma * gamma;
@@ -355,11 +429,8 @@ __device__ __forceinline__ int step_solarprop(Lane<R> &L, const Consts<R> &k, R 
   const R DriftTheta = k.dtheta_sp * pbr * (R(2) + gamma2) * f * inv_g1sq;     // Eq. 36
   dth += DriftTheta * dt * inv_r;
   L.r.add(dr);
-  L.th.add(dth);
+  theta_update(L, dth);
   L.T.add(-dT);
-  if (L.th.v < R(0)) L.th.negate();
-  if (L.th.v > (R)kTwoPi) { L.th.set(L.th.v - (R)kTwoPi); }
-  else if (L.th.v > (R)kPi) { L.th.set((R)kTwoPi - L.th.v); }
   if (L.r.v < R(0)) L.r.negate();
   if (L.r.v > R(100)) return kRecordAndStop;
   return (L.r.v < R(100)) ? kContinue : kStop;

@@ -74,13 +74,17 @@ def test_2d_spectra_match_reference_cpu_model(engine, case):
     z = compare_sections(gpu, ref, [("sp_weber", "sp_weber2", "sp_n"), ("sp_jgr", "sp_jgr2", "sp_n"),
                                     ("sp_burger", "sp_burger2", "sp_n")])
     assert z.size >= 60
-    # per-bin mean weights within Monte Carlo error (the three LIS share particles)
+    # per-bin mean weights within Monte Carlo error (the three LIS share the
+    # particles, so chi^2/dof is taken over the Weber bins).  Tolerances: the
+    # target chi^2/dof <= 1.2; max |z| < 3.5 over the 87 correlated
+    # comparisons (a 3-sigma excursion in one of them is expected a few % of
+    # the time by chance).
     zb = z[: z.size // 3]
     chi2_dof = float(np.mean(zb ** 2))
     print(f"{case}: bins {zb.size}, max|z| {np.abs(z).max():.2f}, chi2/dof {chi2_dof:.3f}, "
           f"within 3 sigma {np.mean(np.abs(z) < 3):.3f}")
-    assert np.abs(z).max() < 4.0
-    assert chi2_dof < 1.6
+    assert np.abs(z).max() < 3.5
+    assert chi2_dof <= 1.2
 
 
 def test_bp_spectra_match_reference_cpu_model(engine):
@@ -90,11 +94,18 @@ def test_bp_spectra_match_reference_cpu_model(engine):
     doc = json.load(open(path))
     sim = sim_from_fixture(doc, 2_000_000, seed=77)
     gpu = spectra_dict(engine.run(sim).spectra[0])
-    z = compare_sections(gpu, doc["spectra"], [("e2_w", "e2_w2", "e2_n")], min_count=100)
+    ref = dict(doc["spectra"])
+    # the reference blocks cover injection ids 0..5999 (energies up to
+    # 60.59 GeV, each id repeated per energy loop, OneDimensionBpCpuModel.cpp:
+    # 63-67): bins only partly covered are left out of the comparison
+    n_ref = np.array(ref["e2_n"], dtype=np.float64)
+    full = n_ref >= 0.9 * np.median(n_ref[n_ref > 0])
+    ref = {k: (np.where(full, np.array(v), 0.0) if k.startswith("e2_") else v) for k, v in ref.items()}
+    z = compare_sections(gpu, ref, [("e2_w", "e2_w2", "e2_n")], min_count=100)
     print(f"bp: bins {z.size}, max|z| {np.abs(z).max():.2f}, chi2/dof {np.mean(z**2):.3f}")
     assert z.size >= 50
-    assert np.abs(z).max() < 4.0
-    assert np.mean(z ** 2) < 1.6
+    assert np.abs(z).max() < 3.5
+    assert np.mean(z ** 2) <= 1.2
 
 
 @pytest.mark.parametrize("model", [abi.GELIO_MODEL_2D_GELIOSPHERE, abi.GELIO_MODEL_2D_SOLARPROP,

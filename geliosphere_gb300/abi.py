@@ -124,6 +124,7 @@ assert ctypes.sizeof(Trajectory) == 40
 PROTOTYPES = {
     "gelio_status_string": (ctypes.c_char_p, [c_int32]),
     "gelio_abi_version": (c_int32, []),
+    "gelio_last_error": (ctypes.c_char_p, []),
     "gelio_create": (c_int32, [POINTER(c_void_p), c_int32]),
     "gelio_destroy": (c_int32, [c_void_p]),
     "gelio_run": (c_int32, [c_void_p, POINTER(SimParams), c_int32, POINTER(RunOpts),
@@ -168,7 +169,12 @@ class GelioError(RuntimeError):
             msg = load().gelio_status_string(status).decode()
         except Exception:  # pragma: no cover - message lookup must not mask the error
             msg = "status %d" % status
-        super().__init__(f"{where}: {msg} (status {status})")
+        detail = ""
+        try:
+            detail = load().gelio_last_error().decode()
+        except Exception:  # pragma: no cover
+            pass
+        super().__init__(f"{where}: {msg} (status {status})" + (f" [{detail}]" if detail else ""))
 
 
 def check(status: int, where: str, allow_warnings: bool = True) -> int:

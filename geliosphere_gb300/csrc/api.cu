@@ -333,18 +333,26 @@ struct gelio_ctx {
   const void *graph_out = nullptr;
   // tuning and last run
   Tuned tuned[4][2];
+  int occ_cache[4][2][8][5] = {};   // [model][precision][block/32 - 1][smem slots]
   gelio_run_stats last{};
   int last_n_slices = 1;
   bool last_timed = false;
 };
 
-static int map_cuda(cudaError_t e) {
+// Text of the last CUDA failure seen by this thread (gelio_last_error).
+static thread_local char g_last_error[256] = "";
+
+static int map_cuda_at(cudaError_t e, int line) {
+  if (e != cudaSuccess)
+    snprintf(g_last_error, sizeof(g_last_error), "%s (%s) at api.cu:%d", cudaGetErrorName(e),
+             cudaGetErrorString(e), line);
   if (e == cudaSuccess) return GELIO_OK;
   if (e == cudaErrorMemoryAllocation) return GELIO_ERR_OUT_OF_MEMORY;
   if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver || e == cudaErrorInvalidDevice)
     return GELIO_ERR_NO_DEVICE;
   return GELIO_ERR_CUDA;
 }
+#define map_cuda(e) map_cuda_at((e), __LINE__)
 
 #define GELIO_TRY(expr)                        \
   do {                                         \
@@ -427,11 +435,18 @@ static int shape_for(gelio_ctx *c, int model, int prec, int n_in_group_hint, con
   if ((size_t)slots * per_slot > (size_t)c->max_smem_optin) slots = 0;
   s.smem_slots = slots;
   s.smem = (size_t)slots * per_slot;
-  const void *k = model_kernel(model, true, prec);
-  GELIO_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem));
-  int occ = 0;
-  GELIO_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, (int)s.block, s.smem));
-  if (occ < 1) return GELIO_ERR_UNSUPPORTED;
+  // occupancy per (model, precision, block, smem slots), cached: no CUDA
+  // call that a stream capture would reject happens while enqueueing
+  const int bi = (int)s.block / 32 - 1;
+  int &cached = c->occ_cache[model][prec ? 1 : 0][bi][slots];
+  if (cached == 0) {
+    const void *k = model_kernel(model, true, prec);
+    int occ = 0;
+    GELIO_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, (int)s.block, s.smem));
+    cached = (occ < 1) ? -1 : occ;
+  }
+  if (cached < 1) return GELIO_ERR_UNSUPPORTED;
+  const int occ = cached;
   int bps = (o && o->blocks_per_sm > 0) ? o->blocks_per_sm : (t.blocks_per_sm > 0 ? t.blocks_per_sm : occ);
   if (bps > occ) bps = occ;
   s.blocks_per_sm = bps;
@@ -458,6 +473,8 @@ const char *gelio_status_string(int32_t s) {
 }
 
 int32_t gelio_abi_version(void) { return GELIO_ABI_VERSION; }
+
+const char *gelio_last_error(void) { return g_last_error; }
 
 int32_t gelio_create(gelio_ctx **out, int32_t device) {
   if (out == nullptr) return GELIO_ERR_INVALID_ARGUMENT;
@@ -487,6 +504,16 @@ int32_t gelio_create(gelio_ctx **out, int32_t device) {
     if ((e = fp_tables(t)) != cudaSuccess || (e = bp_tables(t)) != cudaSuccess ||
         (e = solarprop_tables(t)) != cudaSuccess || (e = geliosphere_tables(t)) != cudaSuccess ||
         (e = set_tables_tu(t)) != cudaSuccess) { rc = map_cuda(e); break; }
+    // dynamic shared memory of the persistent kernels: opt in once, up to the
+    // largest histogram window (4 simulations of a 2D model)
+    for (int m = 0; m < 4 && rc == GELIO_OK; ++m)
+      for (int p = 0; p < 2 && rc == GELIO_OK; ++p) {
+        const int win = (m >= kModelSolarProp) ? 4 * (kWinHi - kWin2DLo) : (kWinHi - kWin1DLo);
+        const int bytes = win * 8 <= c->max_smem_optin ? win * 8 : c->max_smem_optin;
+        e = cudaFuncSetAttribute(model_kernel(m, true, p), cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e != cudaSuccess) rc = map_cuda(e);
+      }
+    if (rc != GELIO_OK) break;
     rc = ensure_sims(c, 16);
   } while (0);
   if (rc != GELIO_OK) {

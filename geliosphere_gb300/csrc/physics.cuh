@@ -227,6 +227,19 @@ __device__ __forceinline__ void phase_normalise(Acc<float> &ph, float &n) {
   ph.set(x);
 }
 
+// sin and cos of the compensated phase v - c (first order in the residual c,
+// |c| <= ulp(v)/2): keeps sin(theta) accurate near theta = pi, where an FP32
+// theta alone is only known to 2.4e-7 rad.
+template <class R>
+__device__ __forceinline__ void phase_sincos(const Acc<R> &ph, R *s, R *c) {
+  Math<R>::sincos(ph.v, s, c);
+  if constexpr (Math<R>::kCompensate) {
+    const R s0 = *s, c0 = *c;
+    *s = fmaf(-ph.c, c0, s0);
+    *c = fmaf(ph.c, s0, c0);
+  }
+}
+
 template <class R>
 __device__ __forceinline__ void theta_update(Lane<R> &L, R dth) {
   if constexpr (sizeof(R) == 8) {
@@ -269,7 +282,7 @@ __device__ __forceinline__ void theta_update(Lane<R> &L, R dth) {
 template <class R>
 __device__ __forceinline__ int step_geliosphere(Lane<R> &L, const Consts<R> &k, R n1, R n2, R n4) {
   using M = Math<R>;
-  const R r = L.r.v, ph = L.th.v, T = L.T.v;
+  const R r = L.r.v, T = L.T.v;
   const R th = theta_full(L);
   const R T0 = (R)kT0;
   const R Tp = T + T0;
@@ -278,7 +291,7 @@ __device__ __forceinline__ int step_geliosphere(Lane<R> &L, const Consts<R> &k, 
   const R inv_Tp = M::rcp(Tp);
   const R beta = P * inv_Tp;
   R s, c;
-  M::sincos(ph, &s, &c);
+  phase_sincos(L.th, &s, &c);
   const R inv_s = M::rcp(s);
   const bool polarA = (th < (R)kThetaLo) || (th > (R)kThetaHi);   // Eq. 25 branch
   const bool nonpolarB = (th > (R)kThetaLo) && (th < (R)kThetaHi);
@@ -379,11 +392,11 @@ __device__ __forceinline__ int step_geliosphere(Lane<R> &L, const Consts<R> &k, 
 template <class R>
 __device__ __forceinline__ int step_solarprop(Lane<R> &L, const Consts<R> &k, R z0, R z1) {
   using M = Math<R>;
-  const R r = L.r.v, ph = L.th.v, T = L.T.v;
+  const R r = L.r.v, T = L.T.v;
   const R th = theta_full(L);
   const R T0 = (R)kT0;
   R s, c;
-  M::sincos(ph, &s, &c);
+  phase_sincos(L.th, &s, &c);
   const R inv_s = M::rcp(s);
   const R gamma = r * k.ov * s;
   const R gamma2 = gamma * gamma;

@@ -239,6 +239,11 @@ typedef struct gelio_ctx gelio_ctx;
 const char *gelio_status_string(int32_t status);
 int32_t gelio_abi_version(void);
 
+/* Text of the last CUDA failure on the calling thread (empty if none):
+ * the CUDA error name and message and where it was raised.  Diagnostics
+ * only; the status codes are the contract. */
+const char *gelio_last_error(void);
+
 /* Create a context on CUDA device `device`.  Returns GELIO_ERR_NO_DEVICE when
  * no CUDA device is usable; there is no CPU fallback. */
 int32_t gelio_create(gelio_ctx **out, int32_t device);

@@ -288,7 +288,7 @@ void gpu_solarprop(const gelio_sim_params &p, uint64_t pid, uint64_t max_steps, 
     const double dKrrTmp = 2.0 * r * omega * omega * sineTheta * sineTheta / (V * V);
     double dKrr = ratio * K0 * beta * Rig * ((2.0 * r * std::sqrt(1.0 + gamma2)) - (r * r * dKrrTmp / (2.0 * std::sqrt(1.0 + gamma2)))) / (1.0 + gamma2);
     dKrr = dKrr + ((1.0 - ratio) * K0 * beta * Rig * ((2.0 * r * std::pow(1.0 + gamma2, 1.5)) - (r * r * dKrrTmp * 3.0 * std::sqrt(1.0 + gamma2) / 2.0)) / std::pow(1.0 + gamma2, 3.0));
-    dKrr = dKrr * 5.0 / (3.0 * 3.4);
+    dKrr = dKrr * 5.0 / (3.0 * (double)3.4f);      // SolarPropLikeModel.cu:120 (FP32 literal)
     const double Bfactor = K.c53 * (r * r) / std::sqrt(1.0 + gamma2);
     const double RigC = (Rig < (double)0.1f) ? (double)0.1f : Rig;
     const double Kpar = K0 * beta * RigC * Bfactor / 3.0;

@@ -148,19 +148,37 @@ def test_batch_equals_single_runs(engine):
             np.testing.assert_allclose(batch[i][k], single[k], rtol=1e-12, err_msg=f"sim {i} {k}")
 
 
-def test_persistent_plain_graph_and_repeat_agree(engine):
-    sim = make_sim(abi.GELIO_MODEL_2D_GELIOSPHERE, 50_000, tilt_deg=20, seed=3,
-                   injection=abi.GELIO_INJ_LOG_GRID, inj_points=100)
+def _consistency_sim():
+    return make_sim(abi.GELIO_MODEL_2D_GELIOSPHERE, 50_000, tilt_deg=20, seed=3,
+                    injection=abi.GELIO_INJ_LOG_GRID, inj_points=100)
+
+
+def _assert_same(a, other):
+    for k in ("grid_n", "sp_n", "n_records", "n_steps", "n_lost"):
+        np.testing.assert_array_equal(a[k], other[k], err_msg=k)
+    np.testing.assert_allclose(a["grid_w"], other["grid_w"], rtol=1e-12)
+
+
+@pytest.mark.parametrize("variant", ["repeat", "plain", "graph", "graph_twice", "small_blocks"])
+def test_launch_variants_agree(engine, variant):
+    """Per-particle random streams make the result independent of the launch
+    shape: persistent vs plain kernel, CUDA graph vs stream, block size and
+    refill interval, repeated runs."""
+    sim = _consistency_sim()
     a = spectra_dict(engine.run(sim).spectra[0])
-    b = spectra_dict(engine.run(sim, plain=True).spectra[0])
-    c = spectra_dict(engine.run(sim, use_graph=True).spectra[0])
-    d = spectra_dict(engine.run(sim, use_graph=True).spectra[0])
-    e = spectra_dict(engine.run(sim, refill=8, block_size=128).spectra[0])
-    for other in (b, c, d, e):
-        for k in ("grid_n", "sp_n", "n_records", "n_steps", "n_lost"):
-            np.testing.assert_array_equal(a[k], other[k], err_msg=k)
-        np.testing.assert_allclose(a["grid_w"], other["grid_w"], rtol=1e-12)
     assert a["n_particles"] == 50_000
+    if variant == "repeat":
+        b = spectra_dict(engine.run(sim).spectra[0])
+    elif variant == "plain":
+        b = spectra_dict(engine.run(sim, plain=True).spectra[0])
+    elif variant == "graph":
+        b = spectra_dict(engine.run(sim, use_graph=True).spectra[0])
+    elif variant == "graph_twice":
+        engine.run(sim, use_graph=True)
+        b = spectra_dict(engine.run(sim, use_graph=True).spectra[0])
+    else:
+        b = spectra_dict(engine.run(sim, refill=8, block_size=128).spectra[0])
+    _assert_same(a, b)
 
 
 def test_fp32_and_fp64_runs_agree(engine):

@@ -543,6 +543,7 @@ static int enqueue_run(gelio_ctx *c, int n, const gelio_run_opts *o, double *d_o
                        size_t rec_cap, bool timed) {
   const int prec = (o && o->precision == GELIO_PREC_FP64) ? 1 : 0;
   const int n_slices = choose_slices(n);
+  (void)cudaGetLastError();   // launch checks below must see only this run's errors
   GELIO_TRY(grow(c->d_part, c->part_bytes, (size_t)n_slices * n * kSpecDoubles * 8));
   GELIO_TRY(cudaMemsetAsync(c->d_ctl, 0, sizeof(Control), st));
   GELIO_TRY(cudaMemsetAsync(c->d_part, 0, (size_t)n_slices * n * kSpecDoubles * 8, st));
@@ -721,7 +722,10 @@ int32_t gelio_run(gelio_ctx *c, const gelio_sim_params *sims, int32_t n, const g
   s.n_records_stored = stored;
   s.n_records_dropped = (int64_t)h.rec_dropped;
   float kms = 0.f;
-  cudaEventElapsedTime(&kms, c->ev_k0, c->ev_k1);
+  if (cudaEventElapsedTime(&kms, c->ev_k0, c->ev_k1) != cudaSuccess) {
+    kms = 0.f;                  // e.g. events replayed from a graph: no kernel time
+    (void)cudaGetLastError();
+  }
   s.kernel_ms = kms;
   s.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   s.block_size = c->last.block_size;
@@ -760,6 +764,7 @@ int32_t gelio_last_stats(gelio_ctx *c, gelio_run_stats *stats) {
   if (c->last_timed) {
     float kms = 0.f;
     if (cudaEventElapsedTime(&kms, c->ev_k0, c->ev_k1) == cudaSuccess) stats->kernel_ms = kms;
+    else (void)cudaGetLastError();
   }
   return (c->h_ctl->status != 0) ? (int)c->h_ctl->status : GELIO_OK;
 }
@@ -774,6 +779,7 @@ int32_t gelio_replay(gelio_ctx *c, const gelio_sim_params *sim, int64_t first, i
   if (count > (int64_t)1 << 31) return GELIO_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lock(c->mu);
   GELIO_TRY(cudaSetDevice(c->device));
+  (void)cudaGetLastError();
   if ((rc = ensure_sims(c, 1)) != GELIO_OK) return rc;
   size_t tb = c->traj_cap * sizeof(gelio_trajectory);
   GELIO_TRY(grow(c->d_traj, tb, (size_t)count * sizeof(gelio_trajectory)));
@@ -825,6 +831,7 @@ int32_t gelio_evaluate(gelio_ctx *c, int32_t model, const double *rows, int64_t 
   GELIO_TRY(cudaMemcpyAsync(c->d_rows, rows, bytes, cudaMemcpyHostToDevice, st));
   GELIO_TRY(cudaMemsetAsync(c->d_part, 0, (size_t)n_slices * kSpecDoubles * 8, st));
   const unsigned grid = (unsigned)((n_rows + 255) / 256);
+  (void)cudaGetLastError();
   k_evaluate<<<grid, 256, 0, st>>>(c->d_rows, n_rows, n_cols, model, n_slices, c->d_part);
   GELIO_TRY(cudaGetLastError());
   k_reduce<<<(kSpecDoubles + 255) / 256, 256, 0, st>>>(c->d_part, n_slices, kSpecDoubles, c->d_out);

@@ -432,9 +432,10 @@ static int shape_for(gelio_ctx *c, int model, int prec, int n_in_group_hint, con
   // shared-memory histogram for up to 4 simulations (2D) / 1 simulation (1D)
   const int max_slots = (model >= kModelSolarProp) ? 4 : 1;
   int slots = (n_in_group_hint >= 1 && n_in_group_hint <= max_slots) ? n_in_group_hint : 0;
-  if ((size_t)slots * per_slot > (size_t)c->max_smem_optin) slots = 0;
+  const size_t qbytes = (size_t)(s.block / 32) * kQueue * sizeof(QEnt);
+  if ((size_t)slots * per_slot + qbytes > (size_t)c->max_smem_optin) slots = 0;
   s.smem_slots = slots;
-  s.smem = (size_t)slots * per_slot;
+  s.smem = (size_t)slots * per_slot + (size_t)(s.block / 32) * kQueue * sizeof(QEnt);
   // occupancy per (model, precision, block, smem slots), cached: no CUDA
   // call that a stream capture would reject happens while enqueueing
   const int bi = (int)s.block / 32 - 1;
@@ -509,7 +510,8 @@ int32_t gelio_create(gelio_ctx **out, int32_t device) {
     for (int m = 0; m < 4 && rc == GELIO_OK; ++m)
       for (int p = 0; p < 2 && rc == GELIO_OK; ++p) {
         const int win = (m >= kModelSolarProp) ? 4 * (kWinHi - kWin2DLo) : (kWinHi - kWin1DLo);
-        const int bytes = win * 8 <= c->max_smem_optin ? win * 8 : c->max_smem_optin;
+        const int need = win * 8 + 8 * kQueue * (int)sizeof(QEnt);
+        const int bytes = need <= c->max_smem_optin ? need : c->max_smem_optin;
         e = cudaFuncSetAttribute(model_kernel(m, true, p), cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         if (e != cudaSuccess) rc = map_cuda(e);
       }

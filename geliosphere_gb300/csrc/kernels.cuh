@@ -277,7 +277,34 @@ __device__ __noinline__ void flush_pending(const KArgs &a, const Sink<MODEL> &si
     }
     sink.add(sl, s, kOffNRecords, cnt);
   }
-  append_records(a, mask, p, MODEL);
+}
+
+// Per-warp queue of exits awaiting evaluation (shared memory).  Lanes push
+// their exit and take a new particle at once; when 32 exits are queued the
+// warp evaluates them with every lane busy, so the FP64 evaluation is paid
+// once per 32 exits instead of once per window with a lane or two active.
+struct QEnt {
+  float Tinj, Texit;
+  int sim;
+  unsigned slot_gbin;        // group slot (low 16 bits), grid bin + 1 (high 16 bits)
+};
+constexpr int kQueue = 64;   // entries per warp (<= 31 left + 32 pushed)
+
+template <int MODEL>
+__device__ __forceinline__ void flush_queue(const KArgs &a, const Sink<MODEL> &sink, const QEnt *q,
+                                            int base, int count) {
+  const int lane = threadIdx.x & 31;
+  const unsigned mask = (count >= 32) ? kFull : ((1u << count) - 1u);
+  if (lane < count) {
+    const QEnt e = q[base + lane];
+    Pending p;
+    p.Tinj = e.Tinj;
+    p.Texit = e.Texit;
+    p.sim = e.sim;
+    p.slot = (int)(e.slot_gbin & 0xffffu);
+    p.gbin = (int)(e.slot_gbin >> 16) - 1;
+    flush_pending<MODEL>(a, sink, mask, p);
+  }
 }
 
 // Direct (non-aggregated) F-p record at a 1 AU crossing.
@@ -372,6 +399,9 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4) ? 2 : 1) k_persistent(co
   const int slots = (gn <= a.smem_slots) ? gn : 0;
   constexpr int W = Window<MODEL>::size;
   for (int i = threadIdx.x; i < slots * W; i += blockDim.x) sh_hist[i] = 0.0;
+  // the exit queues follow the histogram window (sized for a.smem_slots)
+  QEnt *q = reinterpret_cast<QEnt *>(sh_hist + (size_t)a.smem_slots * W) + (threadIdx.x >> 5) * kQueue;
+  int qn = 0;                      // warp-uniform queue length
   __syncthreads();
   Sink<MODEL> sink;
   sink.sh = sh_hist;
@@ -388,12 +418,27 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4) ? 2 : 1) k_persistent(co
   unsigned window = 0;
 
   for (;;) {
-    // 1) evaluate and bin the exits of the last window (warp-aggregated)
+    // 1) queue the exits of the last window; evaluate and bin 32 at a time
     if constexpr (MODEL != kModelFp) {
       const unsigned pm = __ballot_sync(kFull, pending);
       if (pm) {
-        if (pending) flush_pending<MODEL>(a, sink, pm, pd);
-        pending = false;
+        if (pending) {
+          append_records(a, pm, pd, MODEL);
+          QEnt e;
+          e.Tinj = pd.Tinj;
+          e.Texit = pd.Texit;
+          e.sim = pd.sim;
+          e.slot_gbin = ((unsigned)(pd.gbin + 1) << 16) | ((unsigned)pd.slot & 0xffffu);
+          q[qn + __popc(pm & lanemask_lt())] = e;
+          pending = false;
+        }
+        qn += __popc(pm);
+        __syncwarp();
+        if (qn >= 32) {
+          flush_queue<MODEL>(a, sink, q, qn - 32, 32);
+          qn -= 32;
+          __syncwarp();
+        }
       }
     }
     // 2) refill idle lanes from the ticket counter
@@ -436,7 +481,12 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4) ? 2 : 1) k_persistent(co
         }
       }
     }
-    if (!__any_sync(kFull, active)) break;
+    if (!__any_sync(kFull, active)) {
+      if constexpr (MODEL != kModelFp) {
+        if (qn > 0) flush_queue<MODEL>(a, sink, q, 0, qn);
+      }
+      break;
+    }
     // 3) integrate `refill` steps
     constexpr int spc = StepsPerCall<MODEL>::value;
     for (int k = 0; k < a.refill; k += spc) {
@@ -562,7 +612,10 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4) ? 2 : 1) k_plain(const K
   if (valid) sink.add(1 << 30, sim, kOffNSteps, (double)L.steps);
   if constexpr (MODEL != kModelFp) {
     const unsigned pm = __ballot_sync(kFull, pending);
-    if (pending) flush_pending<MODEL>(a, sink, pm, pd);
+    if (pending) {
+      append_records(a, pm, pd, MODEL);
+      flush_pending<MODEL>(a, sink, pm, pd);
+    }
   }
   if (valid && a.replay != nullptr) {
     gelio_trajectory t;

@@ -223,8 +223,8 @@ def main():
     total_traj = sum(s.n_particles for s in sims)
     tune = None
     if not args.no_tune:
-        sample = workload_sims(max(1, min(args.particles, 2_000_000)), rank)[0]
-        tune = eng.autotune(sample)
+        # the production batch with fewer particles per simulation
+        tune = eng.autotune(workload_sims(max(1, min(args.particles, 1_000_000)), rank))
 
     # device-resident inputs for `value`
     raw = bytes((abi.SimParams * n)(*sims))

@@ -87,7 +87,7 @@ class ExitRecord(Structure):
 
 class RunOpts(Structure):
     _fields_ = [
-        ("precision", c_int32), ("plain", c_int32), ("reserved1", c_int32),
+        ("precision", c_int32), ("plain", c_int32), ("compact", c_int32),
         ("block_size", c_int32), ("blocks_per_sm", c_int32), ("refill_interval", c_int32),
         ("use_graph", c_int32), ("reserved0", c_int32), ("max_steps_per_particle", c_uint64),
         ("time_limit_s", c_double), ("records", POINTER(ExitRecord)), ("record_capacity", c_int64),
@@ -135,7 +135,7 @@ PROTOTYPES = {
                                POINTER(Trajectory)]),
     "gelio_evaluate": (c_int32, [c_void_p, c_int32, POINTER(c_double), c_int64, c_int32,
                                  POINTER(Spectra)]),
-    "gelio_autotune": (c_int32, [c_void_p, POINTER(SimParams), POINTER(RunOpts)]),
+    "gelio_autotune": (c_int32, [c_void_p, POINTER(SimParams), c_int32, POINTER(RunOpts)]),
     "gelio_measure_peaks": (c_int32, [c_void_p, POINTER(c_double), POINTER(c_double)]),
 }
 

@@ -293,7 +293,7 @@ using namespace gelio;
 // Context.
 // ---------------------------------------------------------------------------
 struct Tuned {
-  int block = 256, blocks_per_sm = 0, refill = 0;
+  int block = 256, blocks_per_sm = 0, refill = 0, compact = 1;
 };
 
 struct gelio_ctx {
@@ -333,7 +333,7 @@ struct gelio_ctx {
   const void *graph_out = nullptr;
   // tuning and last run
   Tuned tuned[4][2];
-  int occ_cache[4][2][8][5] = {};   // [model][precision][block/32 - 1][smem slots]
+  int occ_cache[4][3][8][5] = {};   // [model][kernel variant][block/32 - 1][smem slots]
   gelio_run_stats last{};
   int last_n_slices = 1;
   bool last_timed = false;
@@ -420,34 +420,62 @@ struct LaunchShape {
   int blocks_per_sm;
 };
 
+// Kernel variant of a run: 1 = FP64, 2 = FP32 compact (<= 85 registers), 0 = FP32.
+static int kernel_variant(const gelio_ctx *c, int model, const gelio_run_opts *o) {
+  if (o && o->precision == GELIO_PREC_FP64) return 1;
+  const int compact = (o && o->compact > 0) ? o->compact : c->tuned[model][0].compact;
+  return compact == 2 ? 2 : 0;
+}
+
 static int shape_for(gelio_ctx *c, int model, int prec, int n_in_group_hint, const gelio_run_opts *o,
                      LaunchShape &s) {
-  const Tuned &t = c->tuned[model][prec ? 1 : 0];
+  const Tuned &t = c->tuned[model][prec == 1 ? 1 : 0];
   s.block = (o && o->block_size > 0) ? (unsigned)o->block_size : (unsigned)t.block;
   if (s.block % 32 != 0 || s.block > 256 || s.block < 32) return GELIO_ERR_INVALID_ARGUMENT;
   s.refill = (o && o->refill_interval > 0) ? o->refill_interval : (t.refill > 0 ? t.refill : default_refill(model));
   if (s.refill % 4 != 0 || s.refill > 4096) return GELIO_ERR_INVALID_ARGUMENT;
   const int win_doubles = (model >= kModelSolarProp) ? (kWinHi - kWin2DLo) : (kWinHi - kWin1DLo);
   const size_t per_slot = (size_t)win_doubles * 8;
-  // shared-memory histogram for up to 4 simulations (2D) / 1 simulation (1D)
-  const int max_slots = (model >= kModelSolarProp) ? 4 : 1;
-  int slots = (n_in_group_hint >= 1 && n_in_group_hint <= max_slots) ? n_in_group_hint : 0;
-  const size_t qbytes = (size_t)(s.block / 32) * kQueue * sizeof(QEnt);
-  if ((size_t)slots * per_slot + qbytes > (size_t)c->max_smem_optin) slots = 0;
-  s.smem_slots = slots;
-  s.smem = (size_t)slots * per_slot + (size_t)(s.block / 32) * kQueue * sizeof(QEnt);
+  const size_t qbytes = (size_t)(s.block / 32) * (kQueue * sizeof(QEnt) + sizeof(int));
   // occupancy per (model, precision, block, smem slots), cached: no CUDA
   // call that a stream capture would reject happens while enqueueing
   const int bi = (int)s.block / 32 - 1;
-  int &cached = c->occ_cache[model][prec ? 1 : 0][bi][slots];
-  if (cached == 0) {
-    const void *k = model_kernel(model, true, prec);
-    int occ = 0;
-    GELIO_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, (int)s.block, s.smem));
-    cached = (occ < 1) ? -1 : occ;
+  const void *kfn = model_kernel(model, true, prec);
+  auto occupancy = [&](int slots_, int &occ_) -> int {
+    int &cached = c->occ_cache[model][prec][bi][slots_];
+    if (cached == 0) {
+      int occ = 0;
+      GELIO_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kfn, (int)s.block,
+                                                              (size_t)slots_ * per_slot + qbytes));
+      cached = (occ < 1) ? -1 : occ;
+    }
+    occ_ = cached;
+    return GELIO_OK;
+  };
+  // shared-memory histograms for up to 4 simulations (2D) / 1 simulation
+  // (1D) of the launch, but never at the cost of resident warps: the slot
+  // count keeps the occupancy that the registers allow
+  int occ0 = 0;
+  int rc0 = occupancy(0, occ0);
+  if (rc0 != GELIO_OK) return rc0;
+  if (occ0 < 1) return GELIO_ERR_UNSUPPORTED;
+  const int max_slots = (model >= kModelSolarProp) ? 4 : 1;
+  int slots = (n_in_group_hint >= 1 && n_in_group_hint <= max_slots) ? n_in_group_hint : 0;
+  while (slots > 0) {
+    if ((size_t)slots * per_slot + qbytes <= (size_t)c->max_smem_optin) {
+      int occs = 0;
+      rc0 = occupancy(slots, occs);
+      if (rc0 != GELIO_OK) return rc0;
+      if (occs >= occ0) break;
+    }
+    slots = (slots == n_in_group_hint) ? 0 : slots - 1;   // all of the group's sims or none
   }
-  if (cached < 1) return GELIO_ERR_UNSUPPORTED;
-  const int occ = cached;
+  s.smem_slots = slots;
+  s.smem = (size_t)slots * per_slot + qbytes;
+  int occ = 0;
+  rc0 = occupancy(slots, occ);
+  if (rc0 != GELIO_OK) return rc0;
+  if (occ < 1) return GELIO_ERR_UNSUPPORTED;
   int bps = (o && o->blocks_per_sm > 0) ? o->blocks_per_sm : (t.blocks_per_sm > 0 ? t.blocks_per_sm : occ);
   if (bps > occ) bps = occ;
   s.blocks_per_sm = bps;
@@ -508,9 +536,9 @@ int32_t gelio_create(gelio_ctx **out, int32_t device) {
     // dynamic shared memory of the persistent kernels: opt in once, up to the
     // largest histogram window (4 simulations of a 2D model)
     for (int m = 0; m < 4 && rc == GELIO_OK; ++m)
-      for (int p = 0; p < 2 && rc == GELIO_OK; ++p) {
+      for (int p = 0; p < 3 && rc == GELIO_OK; ++p) {
         const int win = (m >= kModelSolarProp) ? 4 * (kWinHi - kWin2DLo) : (kWinHi - kWin1DLo);
-        const int need = win * 8 + 8 * kQueue * (int)sizeof(QEnt);
+        const int need = win * 8 + 8 * (kQueue * (int)sizeof(QEnt) + (int)sizeof(int));
         const int bytes = need <= c->max_smem_optin ? need : c->max_smem_optin;
         e = cudaFuncSetAttribute(model_kernel(m, true, p), cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
         if (e != cudaSuccess) rc = map_cuda(e);
@@ -568,6 +596,7 @@ static int enqueue_run(gelio_ctx *c, int n, const gelio_run_opts *o, double *d_o
   a.time_limit_ns = (o && o->time_limit_s > 0.0) ? (unsigned long long)(o->time_limit_s * 1e9) : 0ull;
   if (timed) GELIO_TRY(cudaEventRecord(c->ev_k0, st));
   LaunchShape first{};
+  int variant = prec;
   bool have_first = false;
   for (int m = 0; m < 4; ++m) {
     if (model_mask && !(model_mask & (1u << m))) continue;
@@ -592,11 +621,12 @@ static int enqueue_run(gelio_ctx *c, int n, const gelio_run_opts *o, double *d_o
     }
     LaunchShape s;
     const int hint = model_counts ? model_counts[m] : n;
-    int rc = shape_for(c, m, prec, hint, o, s);
+    variant = kernel_variant(c, m, o);
+    int rc = shape_for(c, m, variant, hint, o, s);
     if (rc != GELIO_OK) return rc;
     a.smem_slots = s.smem_slots;
     a.refill = s.refill;
-    GELIO_TRY(launch_model(m, true, prec, s.grid, s.block, s.smem, st, a));
+    GELIO_TRY(launch_model(m, true, variant, s.grid, s.block, s.smem, st, a));
     if (!have_first) { first = s; have_first = true; }
   }
   if (timed) GELIO_TRY(cudaEventRecord(c->ev_k1, st));
@@ -658,7 +688,8 @@ int32_t gelio_run(gelio_ctx *c, const gelio_sim_params *sims, int32_t n, const g
   }
   cudaStream_t st = c->stream;
   const bool graph = o && o->use_graph && !(o->plain);
-  const unsigned long long key[8] = {(unsigned long long)n, mask, (unsigned long long)(o ? o->precision : 0),
+  const unsigned long long key[8] = {(unsigned long long)n, mask,
+    (unsigned long long)(o ? o->precision : 0) | ((unsigned long long)(o ? o->compact : 0) << 8),
     (unsigned long long)(o ? o->block_size : 0) << 32 | (unsigned)(o ? o->blocks_per_sm : 0),
     (unsigned long long)(o ? o->refill_interval : 0), (unsigned long long)rec_cap,
     (unsigned long long)(o ? o->max_steps_per_particle : 0),
@@ -875,26 +906,41 @@ int32_t gelio_measure_peaks(gelio_ctx *c, double *fp32_tflops, double *xu_gops) 
   return GELIO_OK;
 }
 
-int32_t gelio_autotune(gelio_ctx *c, const gelio_sim_params *sample, gelio_run_opts *best) {
-  if (!c || !sample) return GELIO_ERR_INVALID_ARGUMENT;
-  int rc = validate_params(*sample);
-  if (rc != GELIO_OK) return rc;
-  if (sample->n_particles <= 0) return GELIO_ERR_INVALID_ARGUMENT;
-  const int m = sample->model;
+int32_t gelio_autotune(gelio_ctx *c, const gelio_sim_params *sims, int32_t n, gelio_run_opts *best) {
+  if (!c || !sims || n < 1 || n > kMaxSims) return GELIO_ERR_INVALID_ARGUMENT;
+  int rc;
+  int64_t total = 0;
+  int model = -1;
+  for (int i = 0; i < n; ++i) {
+    if ((rc = validate_params(sims[i])) != GELIO_OK) return rc;
+    total += sims[i].n_particles;
+    if (model < 0 && sims[i].n_particles > 0) model = sims[i].model;
+  }
+  if (total <= 0) return GELIO_ERR_INVALID_ARGUMENT;
   static const int blocks[2] = {128, 256};
-  static const int refills[4] = {4, 8, 16, 32};
+  static const int refills[4] = {8, 16, 32, 64};
+  static const int compacts[2] = {1, 2};
   double best_rate = -1.0;
   gelio_run_opts bo{};
-  std::vector<gelio_spectra> tmp(1);
+  std::vector<gelio_spectra> tmp(n);
+  // one untimed run first (lazy allocations), then every shape once
+  {
+    gelio_run_opts o{};
+    gelio_run_stats s{};
+    rc = gelio_run(c, sims, n, &o, tmp.data(), &s);
+    if (rc != GELIO_OK && rc < GELIO_WARN_FIRST) return rc;
+  }
+  for (int ci = 0; ci < 2; ++ci)
   for (int bi = 0; bi < 2; ++bi) {
     for (int ri = 0; ri < 4; ++ri) {
       gelio_run_opts o{};
+      o.compact = compacts[ci];
       o.block_size = blocks[bi];
       o.refill_interval = refills[ri];
       gelio_run_stats s{};
-      rc = gelio_run(c, sample, 1, &o, tmp.data(), &s);
+      rc = gelio_run(c, sims, n, &o, tmp.data(), &s);
       if (rc != GELIO_OK && rc < GELIO_WARN_FIRST) return rc;
-      const double rate = (s.kernel_ms > 0.0) ? (double)s.n_particles / s.kernel_ms : 0.0;
+      const double rate = (s.kernel_ms > 0.0) ? (double)s.n_steps / s.kernel_ms : 0.0;
       if (rate > best_rate) {
         best_rate = rate;
         bo = o;
@@ -903,10 +949,13 @@ int32_t gelio_autotune(gelio_ctx *c, const gelio_sim_params *sample, gelio_run_o
     }
   }
   std::lock_guard<std::mutex> lock(c->mu);
-  Tuned &t = c->tuned[m][0];
-  t.block = bo.block_size;
-  t.refill = bo.refill_interval;
-  t.blocks_per_sm = 0;
+  if (model >= 0) {
+    Tuned &t = c->tuned[model][0];
+    t.block = bo.block_size;
+    t.refill = bo.refill_interval;
+    t.compact = bo.compact;
+    t.blocks_per_sm = 0;
+  }
   if (best) *best = bo;
   return GELIO_OK;
 }

@@ -185,6 +185,25 @@ __device__ __forceinline__ void append_records(const KArgs &a, unsigned mask, co
   }
 }
 
+// Append one exit record (any lane, no warp synchronisation).
+template <class R>
+__device__ __forceinline__ void append_record_one(const KArgs &a, const Lane<R> &L, int model) {
+  const unsigned long long idx = atomicAdd(&a.ctl->rec_count, 1ull);
+  if (idx < a.record_capacity) {
+    gelio_exit_record rec;
+    rec.particle = (int64_t)L.pid;
+    rec.sim = L.sim;
+    rec.t_injection = L.Tinj;
+    rec.t_exit = (float)L.T.v;
+    rec.r = (float)L.r.v;
+    rec.theta = (model >= kModelSolarProp) ? (float)theta_full(L) : 0.0f;
+    rec.sumac = 0.0f;
+    a.records[idx] = rec;
+  } else {
+    atomicAdd(&a.ctl->rec_dropped, 1ull);
+  }
+}
+
 // Warp-aggregated flush of the pending exits of the lanes in `mask` (all of
 // which execute this call).  Backward models only.
 template <int MODEL>
@@ -388,8 +407,10 @@ __device__ __forceinline__ int find_group_index(const unsigned long long *prefix
 // ---------------------------------------------------------------------------
 // Persistent kernel.
 // ---------------------------------------------------------------------------
-template <int MODEL, class R>
-__global__ void __launch_bounds__(256, (sizeof(R) == 4) ? 2 : 1) k_persistent(const KArgs a) {
+// MINB: CTAs of 256 threads the register budget is sized for (2: <= 128
+// registers; 3: <= 85 registers with some spilling); picked by the autotuner.
+template <int MODEL, class R, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_persistent(const KArgs a) {
   extern __shared__ double sh_hist[];
   const int gn = (int)a.ctl->group_count[MODEL];
   if (gn == 0 || a.ctl->status != 0) return;
@@ -399,9 +420,12 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4) ? 2 : 1) k_persistent(co
   const int slots = (gn <= a.smem_slots) ? gn : 0;
   constexpr int W = Window<MODEL>::size;
   for (int i = threadIdx.x; i < slots * W; i += blockDim.x) sh_hist[i] = 0.0;
-  // the exit queues follow the histogram window (sized for a.smem_slots)
-  QEnt *q = reinterpret_cast<QEnt *>(sh_hist + (size_t)a.smem_slots * W) + (threadIdx.x >> 5) * kQueue;
-  int qn = 0;                      // warp-uniform queue length
+  // the exit queues and their lengths follow the histogram window (sized
+  // for a.smem_slots)
+  QEnt *qbase = reinterpret_cast<QEnt *>(sh_hist + (size_t)a.smem_slots * W);
+  QEnt *q = qbase + (threadIdx.x >> 5) * kQueue;
+  int *qlen = reinterpret_cast<int *>(qbase + (blockDim.x >> 5) * kQueue) + (threadIdx.x >> 5);
+  if ((threadIdx.x & 31) == 0) *qlen = 0;
   __syncthreads();
   Sink<MODEL> sink;
   sink.sh = sh_hist;
@@ -412,33 +436,20 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4) ? 2 : 1) k_persistent(co
   Lane<R> L;
   Consts<R> K;
   SimDev sd;
-  bool active = false, drained = false, pending = false;
-  Pending pd;
+  bool active = false, drained = false;
   int slot = 0, g = -1;
   unsigned window = 0;
 
   for (;;) {
-    // 1) queue the exits of the last window; evaluate and bin 32 at a time
+    // 1) evaluate and bin queued exits, 32 at a time with every lane busy
     if constexpr (MODEL != kModelFp) {
-      const unsigned pm = __ballot_sync(kFull, pending);
-      if (pm) {
-        if (pending) {
-          append_records(a, pm, pd, MODEL);
-          QEnt e;
-          e.Tinj = pd.Tinj;
-          e.Texit = pd.Texit;
-          e.sim = pd.sim;
-          e.slot_gbin = ((unsigned)(pd.gbin + 1) << 16) | ((unsigned)pd.slot & 0xffffu);
-          q[qn + __popc(pm & lanemask_lt())] = e;
-          pending = false;
-        }
-        qn += __popc(pm);
+      __syncwarp();
+      const int qn = *(volatile int *)qlen;
+      if (qn >= 32) {
+        flush_queue<MODEL>(a, sink, q, qn - 32, 32);
         __syncwarp();
-        if (qn >= 32) {
-          flush_queue<MODEL>(a, sink, q, qn - 32, 32);
-          qn -= 32;
-          __syncwarp();
-        }
+        if (lane == 0) *qlen = qn - 32;
+        __syncwarp();
       }
     }
     // 2) refill idle lanes from the ticket counter
@@ -483,6 +494,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4) ? 2 : 1) k_persistent(co
     }
     if (!__any_sync(kFull, active)) {
       if constexpr (MODEL != kModelFp) {
+        const int qn = *(volatile int *)qlen;
         if (qn > 0) flush_queue<MODEL>(a, sink, q, 0, qn);
       }
       break;
@@ -509,15 +521,14 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4) ? 2 : 1) k_persistent(co
                 active = false;
                 sink.add(slot, L.sim, kOffNSteps, (double)L.steps);
                 if (res == kRecordAndStop) {
-                  pending = true;
-                  pd.Tinj = L.Tinj;
-                  pd.Texit = (float)L.T.v;
-                  pd.r = (float)L.r.v;
-                  pd.aux = (float)theta_full(L);
-                  pd.sim = L.sim;
-                  pd.slot = slot;
-                  pd.gbin = L.gbin;
-                  pd.pid = L.pid;
+                  // queue the exit (at most one per lane per window: <= 63 entries)
+                  QEnt e;
+                  e.Tinj = L.Tinj;
+                  e.Texit = (float)L.T.v;
+                  e.sim = L.sim;
+                  e.slot_gbin = ((unsigned)(L.gbin + 1) << 16) | ((unsigned)slot & 0xffffu);
+                  q[atomicAdd(qlen, 1)] = e;
+                  if (a.records != nullptr) append_record_one(a, L, MODEL);
                 } else {
                   sink.add(slot, L.sim, kOffNLost, 1.0);
                 }
@@ -634,22 +645,25 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4) ? 2 : 1) k_plain(const K
 }
 
 // Host-side entry points of one model's translation unit.
+// prec: 0 = FP32 (<= 128 registers), 1 = FP64, 2 = FP32 compact (<= 85 registers)
 #define GELIO_DEFINE_MODEL_ENTRIES(NAME, MODEL)                                              \
   cudaError_t NAME##_launch(bool persistent, int prec, unsigned grid, unsigned block,        \
                             size_t smem, cudaStream_t st, const KArgs &a) {                  \
     if (persistent) {                                                                        \
-      if (prec) k_persistent<MODEL, double><<<grid, block, smem, st>>>(a);                   \
-      else k_persistent<MODEL, float><<<grid, block, smem, st>>>(a);                         \
+      if (prec == 1) k_persistent<MODEL, double, 1><<<grid, block, smem, st>>>(a);           \
+      else if (prec == 2) k_persistent<MODEL, float, 3><<<grid, block, smem, st>>>(a);       \
+      else k_persistent<MODEL, float, 2><<<grid, block, smem, st>>>(a);                      \
     } else {                                                                                 \
-      if (prec) k_plain<MODEL, double><<<grid, block, 0, st>>>(a);                           \
+      if (prec == 1) k_plain<MODEL, double><<<grid, block, 0, st>>>(a);                      \
       else k_plain<MODEL, float><<<grid, block, 0, st>>>(a);                                 \
     }                                                                                        \
     return cudaGetLastError();                                                               \
   }                                                                                          \
   const void *NAME##_kernel(bool persistent, int prec) {                                     \
-    if (persistent) return prec ? (const void *)k_persistent<MODEL, double>                  \
-                                : (const void *)k_persistent<MODEL, float>;                   \
-    return prec ? (const void *)k_plain<MODEL, double> : (const void *)k_plain<MODEL, float>; \
+    if (persistent) return prec == 1 ? (const void *)k_persistent<MODEL, double, 1>          \
+                         : prec == 2 ? (const void *)k_persistent<MODEL, float, 3>           \
+                                     : (const void *)k_persistent<MODEL, float, 2>;          \
+    return prec == 1 ? (const void *)k_plain<MODEL, double> : (const void *)k_plain<MODEL, float>; \
   }                                                                                          \
   cudaError_t NAME##_tables(const BinTables &t) { return set_tables_tu(t); }
 

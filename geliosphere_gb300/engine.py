@@ -142,10 +142,11 @@ class Engine:
 
     @staticmethod
     def opts(precision=0, plain=False, block_size=0, blocks_per_sm=0, refill=0, use_graph=False,
-             max_steps=0, time_limit_s=600.0) -> abi.RunOpts:
+             max_steps=0, time_limit_s=600.0, compact=0) -> abi.RunOpts:
         o = abi.RunOpts()
         o.precision = precision
         o.plain = 1 if plain else 0
+        o.compact = compact
         o.block_size = block_size
         o.blocks_per_sm = blocks_per_sm
         o.refill_interval = refill
@@ -207,9 +208,11 @@ class Engine:
         abi.check(self.lib.gelio_measure_peaks(self.ctx, byref(f), byref(x)), "gelio_measure_peaks")
         return f.value, x.value
 
-    def autotune(self, sample: abi.SimParams) -> abi.RunOpts:
+    def autotune(self, sample) -> abi.RunOpts:
+        sims = [sample] if isinstance(sample, abi.SimParams) else list(sample)
+        arr = (abi.SimParams * len(sims))(*sims)
         best = abi.RunOpts()
-        abi.check(self.lib.gelio_autotune(self.ctx, byref(sample), byref(best)), "gelio_autotune")
+        abi.check(self.lib.gelio_autotune(self.ctx, arr, len(sims), byref(best)), "gelio_autotune")
         return best
 
 

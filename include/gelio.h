@@ -192,7 +192,9 @@ typedef struct gelio_run_opts {
                                      (default); 1 = one thread per particle, one
                                      launch per simulation, no refill (the plain
                                      baseline kernel) */
-    int32_t reserved1;
+    int32_t compact;              /* FP32 persistent kernel register budget: 0 = tuned
+                                     default, 1 = <= 128 registers (2 CTAs of 256 per
+                                     SM), 2 = <= 85 registers (3 CTAs of 256 per SM) */
     int32_t block_size;           /* 0 = tuned default */
     int32_t blocks_per_sm;        /* 0 = occupancy maximum */
     int32_t refill_interval;      /* steps between warp refills (multiple of 4); 0 = tuned */
@@ -282,10 +284,12 @@ int32_t gelio_replay(gelio_ctx *ctx, const gelio_sim_params *sim,
 int32_t gelio_evaluate(gelio_ctx *ctx, int32_t model, const double *rows,
                        int64_t n_rows, int32_t n_cols, gelio_spectra *out);
 
-/* Pick block size, blocks per SM and refill interval for one model by timing
- * short runs of `sample` (n_particles taken from it) and store the choice in
- * the context; the chosen options are written to *best (host). */
-int32_t gelio_autotune(gelio_ctx *ctx, const gelio_sim_params *sample,
+/* Pick the block size and refill interval by timing short runs of a sample
+ * batch (n simulations, typically the production batch with fewer particles
+ * each) and store the choice in the context for the model of the first
+ * non-empty simulation; the chosen options are written to *best (host).
+ * The figure of merit is particle-steps per second of the SDE kernels. */
+int32_t gelio_autotune(gelio_ctx *ctx, const gelio_sim_params *sims, int32_t n,
                        gelio_run_opts *best);
 
 /* Measure this device's FP32 SIMT throughput (FMA chains; FLOP/s with an

@@ -109,7 +109,7 @@ def test_async_device_api_matches_host_api(engine):
 
 def test_autotune_picks_a_valid_shape(engine):
     best = engine.autotune(make_sim(abi.GELIO_MODEL_2D_GELIOSPHERE, 200_000, seed=5))
-    assert best.block_size in (128, 256) and best.refill_interval in (4, 8, 16, 32)
+    assert best.block_size in (128, 256) and best.refill_interval in (8, 16, 32, 64)
     assert engine.run(make_sim(abi.GELIO_MODEL_2D_GELIOSPHERE, 1000)).status == abi.GELIO_OK
 
 

@@ -46,6 +46,8 @@ GELIO_PREC_FP64 = 1
 
 GELIO_FLAG_SOLARPROP_THETA_DRIFT_POLARITY = 0x1
 GELIO_GRID_MAX = 320
+GELIO_NOALLOC_MAX_SIMS = 8
+GELIO_NOALLOC_SCRATCH_BYTES = 1049344
 
 
 class SimParams(Structure):
@@ -137,6 +139,7 @@ PROTOTYPES = {
                                  POINTER(Spectra)]),
     "gelio_autotune": (c_int32, [c_void_p, POINTER(SimParams), c_int32, POINTER(RunOpts)]),
     "gelio_measure_peaks": (c_int32, [c_void_p, POINTER(c_double), POINTER(c_double)]),
+    "gelio_run_noalloc": (c_int32, [c_void_p, c_int32, POINTER(RunOpts), c_void_p, c_void_p]),
 }
 
 _LIB = None

@@ -17,7 +17,7 @@ OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB = os.path.join(OUT_DIR, "libgelio_cuda.so")
 
-UNITS = ["api.cu", "k_fp.cu", "k_bp.cu", "k_solarprop.cu", "k_geliosphere.cu"]
+UNITS = ["api.cu", "k_fp.cu", "k_bp.cu", "k_solarprop.cu", "k_geliosphere.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # FP32 SDE steps: flush denormals, approximate division/sqrt where the
 # kernels ask for them; the bit-exact parts use explicit _rn intrinsics.

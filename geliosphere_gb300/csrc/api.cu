@@ -250,10 +250,23 @@ __global__ void k_peak_xu(float *out, int iters) {
   if (s == 123.456f) out[0] = s;
 }
 
+// Launch wrappers for the allocation-free entry point (noalloc.cu), which
+// runs the same sequence on its own static scratch.
+cudaError_t launch_prepare(const gelio_sim_params *p, int n, SimDev *sims, float *tables, Groups g,
+                           Control *ctl, cudaStream_t st) {
+  k_prepare<<<1, 256, 0, st>>>(p, n, sims, tables, g, ctl);
+  return cudaGetLastError();
+}
+cudaError_t launch_reduce(const double *part, int n_slices, long long n_total, double *out,
+                          cudaStream_t st) {
+  k_reduce<<<(unsigned)((n_total + 255) / 256), 256, 0, st>>>(part, n_slices, n_total, out);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // Host tables from the reference definitions.
 // ---------------------------------------------------------------------------
-static void build_tables(BinTables &t) {
+void build_tables(BinTables &t) {
   static const double sp[32] = {0, 0.01, 0.015, 0.0225, 0.03375, 0.050625,
     0.0759375, 0.113906, 0.170859, 0.256289, 0.384434, 0.57665,
     0.864976, 1.29746, 1.9462, 2.91929, 4.37894, 6.56841, 9.85261,

@@ -292,6 +292,29 @@ int32_t gelio_evaluate(gelio_ctx *ctx, int32_t model, const double *rows,
 int32_t gelio_autotune(gelio_ctx *ctx, const gelio_sim_params *sims, int32_t n,
                        gelio_run_opts *best);
 
+/* Run n_sims (<= GELIO_NOALLOC_MAX_SIMS) simulations without allocating any
+ * memory.  No counterpart in the reference: it serves callers that cannot
+ * call cudaMalloc -- code that runs where device allocation is not allowed
+ * or not wanted, such as a host application with a fixed device-memory
+ * budget or a plugin that must not own allocations.  The caller passes the
+ * inputs and outputs in device memory (d_sims: n_sims gelio_sim_params;
+ * d_out: n_sims gelio_spectra) and a stream (NULL = the legacy default
+ * stream); no context is needed.  All scratch lives in one static device
+ * array of GELIO_NOALLOC_SCRATCH_BYTES that every GPU loading the library
+ * holds until the process exits.  The first call on a device sets that
+ * device up (resolves the array's address, fills tables, queries
+ * occupancy), so it should be made before any stream capture.  Calls share the
+ * array: calls that overlap on the GPU (other streams, other threads) race
+ * and corrupt each other.  The call waits for its own work on `stream` and
+ * returns its status.  Exit records and the plain kernel are not available
+ * here (GELIO_ERR_UNSUPPORTED); more than GELIO_NOALLOC_MAX_SIMS simulations
+ * is GELIO_ERR_INVALID_ARGUMENT. */
+#define GELIO_NOALLOC_MAX_SIMS 8
+#define GELIO_NOALLOC_SCRATCH_BYTES 1049344
+int32_t gelio_run_noalloc(const gelio_sim_params *d_sims, int32_t n_sims,
+                          const gelio_run_opts *opts, gelio_spectra *d_out,
+                          void *stream);
+
 /* Measure this device's FP32 SIMT throughput (FMA chains; FLOP/s with an
  * FMA counted as 2) and special-function-unit throughput (ex2.approx chains,
  * operations/s), in TFLOP/s and Gop/s.  A measurement helper for rooflines;

@@ -76,3 +76,17 @@ def test_no_device_is_an_error_not_a_fallback(lib):
     with pytest.raises(abi.GelioError):
         from geliosphere_gb300 import Engine
         Engine(0)
+
+
+def test_host_library_exports_every_declared_symbol():
+    from geliosphere_gb300 import host
+    host.build()
+    lib = host.load()
+    names = declared_functions(os.path.join(ROOT, "include", "gelio_host.h"))
+    assert len(names) >= 10
+    out = subprocess.run(["nm", "-D", "--defined-only", host.LIB], capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r" T (gelio_host_\w+)", out))
+    missing = [n for n in names if n.startswith("gelio_host_") and n not in exported]
+    assert not missing, missing
+    for n in names:
+        assert hasattr(lib, n)

@@ -1,0 +1,195 @@
+"""Host drop-in layer on the CPU: the C++ spectrum writers reproduce the
+reference evaluators' files byte for byte (.dat and .csv) for the spectra
+the oracle bins from the committed log.dat fixtures; argument parsing,
+settings and parameter resolution follow the reference's precedence.
+No GPU is touched: these functions never create an engine context."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from geliosphere_gb300 import abi
+
+host = pytest.importorskip("geliosphere_gb300.host")
+
+FILES = {
+    "2d": ["Usoskin_2005", "Weber", "Burger", "Ulysses", "Ams"],
+    "bp": ["output_1e3bin", "output_1e2bin", "output_logbin", "output_4e2bin"],
+    "fp": ["output_1e3bin", "output_1e2bin", "output_logbin", "output_4e2bin"],
+}
+MODEL_ID = {"fp": 0, "bp": 1, "2d": 3}
+
+
+@pytest.fixture(scope="module")
+def hlib():
+    if not os.path.exists(host.LIB):
+        host.build()
+    return host.load()
+
+
+@pytest.fixture()
+def fresh(hlib):
+    hlib.gelio_host_reset()
+    yield hlib
+    hlib.gelio_host_reset()
+
+
+def read_log(path):
+    rows = [[float(x) for x in ln.split()] for ln in open(path) if ln.strip()]
+    return np.array(rows[:-1])   # countLines() - 1 records
+
+
+@pytest.mark.parametrize("model", ["2d", "bp", "fp"])
+@pytest.mark.parametrize("csv", [0, 1])
+def test_writer_bytes_match_reference(oracle, hlib, tmp_path, model, csv):
+    d = os.path.join(GOLDEN, f"eval_{model}")
+    s = oracle.evaluate(MODEL_ID[model], read_log(os.path.join(d, "log.dat")))
+    assert hlib.gelio_host_write_spectra(MODEL_ID[model], ctypes.byref(s), csv, str(tmp_path).encode()) == 0
+    ext = ".csv" if csv else ".dat"
+    for name in FILES[model]:
+        got = open(tmp_path / (name + ext), "rb").read()
+        exp = open(os.path.join(d, name + ext), "rb").read()
+        assert got == exp, f"{name}{ext} differs"
+
+
+def test_parse_defaults_and_quirks(fresh):
+    # no model flag -> "1D Fp"; no -s -> default settings never loaded
+    assert host.parse([]) == 1
+    assert host.get_string("model", "1D Fp") == "1D Fp"
+    assert fresh.gelio_host_get_int(b"run_simulation", -7) == 1
+    assert fresh.gelio_host_get_float(b"K0_default", -1.0) == -1.0
+
+
+def test_parse_values_and_conversions(fresh):
+    assert host.parse(["-T", "-K", "5e22", "-V", "400", "-d", "50", "-N", "3", "-p", "x", "-c"]) == 1
+    assert host.get_string("model") == "2D Geliosphere"
+    assert fresh.gelio_host_get_float(b"K0", 0) == np.float32(np.float32(5e22) * 4.4683705e-27)
+    assert fresh.gelio_host_get_float(b"V", 0) == np.float32(np.float32(400.0) * 6.68458712e-9)
+    assert fresh.gelio_host_get_int(b"K0_entered_by_user", 0) == 1
+    assert fresh.gelio_host_get_int(b"millions", 0) == 3
+    assert fresh.gelio_host_get_int(b"csv", 0) == 1
+    assert host.get_string("destination") == "x"
+    assert host.get_string("K0input") == "5e+22"
+
+
+@pytest.mark.parametrize("args", [["-F", "-B"], ["-K", "5e22", "-m", "1", "-y", "2000"],
+                                  ["-b", "x.csv", "-N", "2"], ["-m", "3"], ["-d", "1"], ["-V", "50"],
+                                  ["-K", "-1"], ["-N", "0"], ["--nope"]])
+def test_parse_rejections(fresh, args):
+    assert host.parse(args) != 1
+
+
+def test_batch_flag_returns_early(fresh):
+    assert host.parse(["-b", "rows.csv"]) == 1
+    assert host.get_string("model") == "batch run"
+    assert host.get_string("inputBatchFile") == "rows.csv"
+
+
+def test_settings_and_resolution(fresh, tmp_path):
+    st = tmp_path / "Settings.toml"
+    st.write_text("""[default_values]
+K0 = 5e22
+V = 400.0
+dt = 50.0
+r_injection = 1.0
+uniform_energy_injection_maximum = 101.0
+
+[2d_models_common_settings]
+theta_injection = 90.0
+use_uniform_injection = false
+
+[SolarProp_like_model_settings]
+SolarProp_ratio = 0.02
+
+[Geliosphere_model_settings]
+Geliosphere_ratio = 0.2
+K0_ratio = 1.0
+C_delta = 8.7e-5
+default_tilt_angle = 0.1
+
+[advanced_settings]
+remove_log_files_after_simulation = true
+""")
+    assert host.parse(["-T", "-s", str(st)]) == 1
+    sim = abi.SimParams()
+    assert fresh.gelio_host_resolve(abi.GELIO_MODEL_2D_GELIOSPHERE, ctypes.byref(sim)) == 0
+    k0 = np.float32(5e22 * 4.4683705e-27)
+    assert np.float32(sim.K0) == np.float32(k0 * np.float32(1.0))
+    assert np.float32(sim.V) == np.float32(400.0 * 6.68458712e-9)
+    assert sim.dt == 50.0
+    assert sim.injection == abi.GELIO_INJ_SOLARPROP_GRID
+    assert np.float32(sim.tilt) == np.float32(np.float32(0.1) * np.float32(3.1415926535) / np.float32(180.0))
+    assert np.float32(sim.ratio) == np.float32(0.2)
+    # 1 million rounds up to whole chunks of 4096
+    assert sim.n_particles == -(-1_000_000 // 4096) * 4096
+
+
+def test_resolution_user_k0_wins_over_ratio(fresh):
+    assert host.parse(["-T", "-K", "1e22"]) == 1
+    sim = abi.SimParams()
+    fresh.gelio_host_resolve(abi.GELIO_MODEL_2D_GELIOSPHERE, ctypes.byref(sim))
+    assert np.float32(sim.K0) == np.float32(np.float32(1e22) * 4.4683705e-27)
+
+
+def test_resolution_backward_defaults(fresh):
+    assert host.parse(["-B"]) == 1
+    sim = abi.SimParams()
+    fresh.gelio_host_resolve(abi.GELIO_MODEL_1D_BP, ctypes.byref(sim))
+    # __constant__ defaults: dt 5, K0 0.000222, V 2.66667e-6 (sign applied by the engine)
+    assert (np.float32(sim.dt), np.float32(sim.K0), np.float32(sim.V)) == (
+        np.float32(5.0), np.float32(0.000222), np.float32(2.66667e-6))
+
+
+def test_put_semantics(fresh):
+    fresh.gelio_host_put_int(b"a", 1)
+    fresh.gelio_host_put_int(b"a", 2)        # numbers: insert, no overwrite
+    fresh.gelio_host_put_string(b"s", b"x")
+    fresh.gelio_host_put_string(b"s", b"y")  # strings overwrite
+    assert fresh.gelio_host_get_int(b"a", 0) == 1
+    assert host.get_string("s") == "y"
+
+
+@pytest.mark.parametrize("month,year,expect", [(5, 1976, 1642), (6, 1976, 1643), (1, 2000, 1958)])
+def test_carrington_rotation(hlib, month, year, expect):
+    assert hlib.gelio_host_carrington_rotation(month, year) == expect
+
+
+def test_log_line_formats(hlib):
+    r = abi.ExitRecord()
+    r.particle, r.sim, r.t_injection, r.t_exit, r.r, r.theta, r.sumac = 3, 0, 1.5, 0.75, 100.0, 1.25, 0.5
+    buf = ctypes.create_string_buffer(256)
+    hlib.gelio_host_log_line(abi.GELIO_MODEL_1D_BP, ctypes.byref(r), 0.0, buf, 256)
+    f = buf.value.decode().split()
+    assert f[0] == "0.75" and f[1] == "1.5" and f[2] == "100"
+    hlib.gelio_host_log_line(abi.GELIO_MODEL_2D_GELIOSPHERE, ctypes.byref(r), np.float32(np.pi / 2), buf, 256)
+    f = buf.value.decode().split()
+    assert len(f) == 6 and f[0] == "1.5" and f[1] == "0.75" and f[5] == "1.25"
+
+
+def _parse_at(app_dir, args):
+    n, arr = host.argv([os.path.join(str(app_dir), "geliosphere"), *args])
+    return host.load().gelio_host_parse(n, arr)
+
+
+def test_month_year_lookup_1d(fresh, tmp_path):
+    # synthetic table with the reference's columns (K0_phi_table.csv layout)
+    (tmp_path / "K0_phi_table.csv").write_text(
+        "year_week,moodulation_potentional,k0_au2/s,k0_m2/s,V,year,month\n"
+        "2001.04,700,1.5E-004,3.0E+018,450,2001,1\n"
+        "2001.12,710,1.25E-004,3.1E+018,500,2001,2\n")
+    assert _parse_at(tmp_path, ["-B", "-m", "2", "-y", "2001"]) == 1
+    assert fresh.gelio_host_get_float(b"K0", 0) == np.float32(1.25e-4)
+    assert fresh.gelio_host_get_float(b"V", 0) == np.float32(500.0 * 6.68458712e-9)
+    assert fresh.gelio_host_get_int(b"month_option", 0) == 2
+
+
+def test_month_year_lookup_2d(fresh, tmp_path):
+    (tmp_path / "Geliosphere_K0_phi_table.csv").write_text(
+        "carrington_rotation,year_week,modulation_potentional,k0_au2/s,tilt_angle,year,month,day,polarity\n"
+        "1958,2000.0027322,752,2.5E-05,73.9,2000,1,1,-1\n")
+    assert _parse_at(tmp_path, ["-T", "-m", "1", "-y", "2000"]) == 1
+    assert fresh.gelio_host_get_float(b"K0", 0) == np.float32(2.5e-5)
+    assert fresh.gelio_host_get_float(b"tilt_angle", 0) == np.float32(73.9)
+    assert fresh.gelio_host_get_int(b"polarity", 0) == -1

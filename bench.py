@@ -52,9 +52,20 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gelio", choices=["gelio", "reference"])
-    ap.add_argument("--particles", type=int, default=10_000_000, help="particles per case")
+    ap.add_argument("--particles", type=int, default=None,
+                    help="particles per case (default 1e7; 1e6 for the F-p workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--surr-train", type=int, default=20000, help="surrogate: training spectra")
+    ap.add_argument("--surr-train-particles", type=int, default=500_000)
+    ap.add_argument("--surr-test", type=int, default=2000, help="surrogate: held-out parameter draws")
+    ap.add_argument("--surr-test-particles", type=int, default=10_000_000)
+    ap.add_argument("--surr-epochs", type=int, default=40)
+    ap.add_argument("--workload", default="geliosphere", choices=["geliosphere", "bp", "fp", "batch256", "surrogate"],
+                    help="geliosphere: the headline 4-case 2D run (default); bp: 1D B-p 1e7 on a 100-point "
+                         "log grid, FP32 and FP64 steps; fp: 1D F-p 1e6 log-uniform, 300 log bins; batch256: "
+                         "256 random 2D simulations in one launch vs 256 plain launches; surrogate: train the "
+                         "MLP ensemble on MC spectra and time it against the MC on held-out draws")
     return ap.parse_args()
 
 
@@ -73,6 +84,39 @@ def workload_sims(n_per_case: int, rank: int):
                              r_injection=1.0, theta_deg=90.0, tilt_deg=tilt, polarity=pol,
                              injection=abi.GELIO_INJ_LOG_GRID, inj_min=0.01, inj_max=100.0,
                              inj_points=100, seed=1_000_003 * (rank + 1) + 17 * i))
+    return sims
+
+
+def workload_1d(model: int, n: int, rank: int):
+    """1D B-p: 1e7 protons from r = 1 AU on a 100-point log grid 0.01-100 GeV;
+    1D F-p: 1e6 protons from r = 100 AU, log-uniform 0.01-200 GeV, 300 log
+    bins at 1 AU; K0 = 5e22 cm^2/s, V = 400 km/s, dt = 50 s."""
+    from geliosphere_gb300 import abi, make_sim
+    if model == abi.GELIO_MODEL_1D_BP:
+        return [make_sim(model, n, K0_cm2s=5e22, V_kms=400.0, dt=50.0, r_injection=1.0,
+                         injection=abi.GELIO_INJ_LOG_GRID, inj_min=0.01, inj_max=100.0, inj_points=100,
+                         seed=7_000_001 * (rank + 1))]
+    return [make_sim(model, n, K0_cm2s=5e22, V_kms=400.0, dt=50.0, injection=abi.GELIO_INJ_LOG_UNIFORM,
+                     inj_min=0.01, inj_max=200.0, grid_min=0.01, grid_max=200.0, grid_bins=300,
+                     seed=9_000_001 * (rank + 1))]
+
+
+def workload_batch256(rank: int, scale: float = 1.0):
+    """256 2D Geliosphere simulations drawn from one seed: N log-uniform in
+    [0.1, 5] x 1e6, K0 U[1e22, 1e23] cm^2/s, V U[350, 750] km/s, tilt U[5, 75]
+    deg, polarity +/-1, r U[1, 80] AU, theta U[10, 170] deg, dt = 500 s, each
+    on the 100-point log grid 0.01-100 GeV."""
+    import numpy as np
+    from geliosphere_gb300 import abi, make_sim
+    rng = np.random.default_rng(20240 + rank)
+    sims = []
+    for i in range(256):
+        n = int(np.exp(rng.uniform(np.log(0.1), np.log(5.0))) * 1e6 * scale)
+        sims.append(make_sim(abi.GELIO_MODEL_2D_GELIOSPHERE, max(n, 1), K0_cm2s=float(rng.uniform(1e22, 1e23)),
+                             V_kms=float(rng.uniform(350, 750)), dt=500.0, tilt_deg=float(rng.uniform(5, 75)),
+                             polarity=int(rng.choice([-1, 1])), r_injection=float(rng.uniform(1, 80)),
+                             theta_deg=float(rng.uniform(10, 170)), injection=abi.GELIO_INJ_LOG_GRID,
+                             inj_min=0.01, inj_max=100.0, inj_points=100, seed=int(rng.integers(1, 2**62))))
     return sims
 
 
@@ -197,6 +241,151 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_batch256(args, eng, rank, world, local):
+    """256 random 2D simulations (uneven N and parameters): the persistent
+    kernel inside a captured CUDA graph, all 256 in one launch, against the
+    plain one-thread-per-particle kernel launched once per simulation."""
+    import ctypes
+    import torch
+    from geliosphere_gb300 import abi
+    sims = workload_batch256(rank)
+    n = len(sims)
+    total = sum(s.n_particles for s in sims)
+    tune = None if args.no_tune else eng.autotune(workload_batch256(rank, scale=0.05))
+    out = (abi.Spectra * n)()
+    for _ in range(max(1, args.warmup)):
+        eng.run(sims, out=out, use_graph=True)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    times = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r = eng.run(sims, out=out, use_graph=True)
+            times.append(time.perf_counter() - t0)
+    assert r.stats.n_particles == total, "incomplete batch"
+    persistent = total * args.steps / sum(times)
+    # plain arm: one launch per simulation, 256 launches in sequence
+    flush.zero_()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rp = eng.run(sims, plain=True)
+    t_plain = time.perf_counter() - t0
+    plain = total / t_plain
+    if rank != 0:
+        return
+    line = {"metric": "batched 2D Geliosphere trajectories/s", "value": persistent, "unit": "trajectories/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * sum(times) / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": workload_batch256.__doc__.replace("\n", " "), "simulations": n,
+                       "particles": total, "graph": True,
+                       "tuned": {"block": tune.block_size, "refill": tune.refill_interval} if tune else None,
+                       "l2": "flushed between timed steps (256 MiB write)"},
+            "e2e": {"value": persistent, "unit": "trajectories/s",
+                    "h2d_bytes_per_step": n * ctypes.sizeof(abi.SimParams),
+                    "d2h_bytes_per_step": n * ctypes.sizeof(abi.Spectra)},
+            "plain": {"value": plain, "unit": "trajectories/s", "launches": n, "seconds": t_plain,
+                      "steps": int(rp.stats.n_steps)},
+            "persistent_over_plain": persistent / plain,
+            "particle_steps_per_s": r.stats.n_steps / (sum(times) / args.steps),
+            "gpu_launches": 3 * args.steps, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
+def random_2d_sims(n: int, particles: int, seed: int):
+    """2D Geliosphere simulations over the batch parameter ranges (K0 U[1e22,
+    1e23] cm^2/s, V U[350, 750] km/s, tilt U[5, 75] deg, polarity +/-1, r
+    U[1, 80] AU, theta U[10, 170] deg, dt = 500 s), each on the 100-point log
+    grid 0.01-100 GeV."""
+    import numpy as np
+    from geliosphere_gb300 import abi, make_sim
+    rng = np.random.default_rng(seed)
+    return [make_sim(abi.GELIO_MODEL_2D_GELIOSPHERE, particles, K0_cm2s=float(rng.uniform(1e22, 1e23)),
+                     V_kms=float(rng.uniform(350, 750)), dt=500.0, tilt_deg=float(rng.uniform(5, 75)),
+                     polarity=int(rng.choice([-1, 1])), r_injection=float(rng.uniform(1, 80)),
+                     theta_deg=float(rng.uniform(10, 170)), injection=abi.GELIO_INJ_LOG_GRID, inj_min=0.01,
+                     inj_max=100.0, inj_points=100, seed=int(rng.integers(1, 2**62))) for _ in range(n)]
+
+
+def run_surrogate(args, eng, rank, world, local):
+    """Learned surrogate: an ensemble of 5 MLPs (7 -> 256 x 4 -> 1, SiLU, BF16
+    weights, FP32 accumulation) trained on the GPU on MC spectra of random 2D
+    simulations, evaluated on held-out draws against high-statistics MC:
+    spectra/s of each, median |delta flux| over 0.1-10 GeV, fallback rate."""
+    import numpy as np
+    from geliosphere_gb300 import surrogate as sg
+    chunk = 256
+    t0 = time.perf_counter()
+    train = random_2d_sims(args.surr_train, args.surr_train_particles, 31 + rank)
+    sur = sg.Surrogate(eng, members=5, batch_rows=16384, seed=7 + rank)
+    train_err = []
+    for k in range(0, len(train), chunk):
+        part = train[k:k + chunk]
+        res = eng.run(part)
+        sur.add_spectra(part, res.spectra)
+    t_data = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    loss = sur.train(args.surr_epochs)
+    t_train = time.perf_counter() - t1
+    test = random_2d_sims(args.surr_test, args.surr_test_particles, 10_000 + rank)
+    # Monte Carlo answer for every held-out draw (the judge of the error)
+    mc_s, ref = 0.0, []
+    low = []
+    for k in range(0, len(test), chunk):
+        part = test[k:k + chunk]
+        t2 = time.perf_counter()
+        res = eng.run(part)
+        mc_s += time.perf_counter() - t2
+        ref += [sg.mc_ln_ratio(res.spectra[i], part[i], lis=1, min_count=100) for i in range(len(part))]
+    # the same draws at the training statistics: what the MC alone gives at that cost
+    small = [sim for sim in test[:min(len(test), 200)]]
+    for sim in small:
+        sim.n_particles = args.surr_train_particles
+    res_small = eng.run(small)
+    low = [sg.mc_ln_ratio(res_small.spectra[i], small[i], lis=1, min_count=1) for i in range(len(small))]
+    for sim in small:
+        sim.n_particles = args.surr_test_particles
+    # surrogate: warm-up, then timed
+    sur.predict(test[:chunk])
+    t3 = time.perf_counter()
+    pred, sd = sur.predict(test)
+    t_pred = time.perf_counter() - t3
+    errs, errs_mc, fb = [], [], 0
+    for i, sim in enumerate(test):
+        T = sg.grid_energies(sim)
+        sel = (T >= 0.1) & (T <= 10.0) & np.isfinite(ref[i])
+        errs.append(np.abs(np.exp(pred[i][sel] - ref[i][sel]) - 1.0))
+        fb += int(np.max(sd[i][(T >= 0.1) & (T <= 10.0)]) > 0.03)
+        if i < len(low):
+            sel2 = sel & np.isfinite(low[i])
+            errs_mc.append(np.abs(np.exp(low[i][sel2] - ref[i][sel2]) - 1.0))
+    med = float(np.median(np.concatenate(errs)))
+    med_mc = float(np.median(np.concatenate(errs_mc)))
+    sur_rate = len(test) / t_pred
+    mc_rate = len(test) / mc_s
+    if rank != 0:
+        return
+    line = {"metric": "surrogate spectra/s", "value": sur_rate, "unit": "spectra/s", "n_gpus": world,
+            "steps": 1, "warmup": 1, "ms_per_step": 1e3 * t_pred, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": run_surrogate.__doc__.replace("\n", " "),
+                       "train_spectra": len(train), "train_particles": args.surr_train_particles,
+                       "test_draws": len(test), "test_particles": args.surr_test_particles,
+                       "epochs": args.surr_epochs, "members": 5, "lis": "Usoskin 2005"},
+            "mc_spectra_per_s": mc_rate, "surrogate_over_mc": sur_rate / mc_rate,
+            "median_abs_dflux_0p1_10GeV": med,
+            "mc_at_training_statistics_median_abs_dflux": med_mc,
+            "fallback_fraction": fb / len(test),
+            "train_loss": [float(v) for v in loss], "seconds": {"mc_training_data": t_data, "training": t_train,
+                                                                 "mc_test": mc_s, "surrogate_predict": t_pred},
+            "e2e": {"value": sur_rate, "unit": "spectra/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": None}
+    print(json.dumps(line), flush=True)
+    sur.close()
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
@@ -218,13 +407,33 @@ def main():
 
     torch.cuda.set_device(local)
     eng = Engine(local)
-    sims = workload_sims(args.particles, rank)
+    if args.workload in ("batch256", "surrogate"):
+        (run_batch256 if args.workload == "batch256" else run_surrogate)(args, eng, rank, world, local)
+        eng.close()
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+    if args.particles is None:
+        args.particles = 1_000_000 if args.workload == "fp" else 10_000_000
+    headline = args.workload == "geliosphere"
+    if headline:
+        metric, config = "2D Geliosphere trajectories/s", dict(CONFIG)
+        make = lambda n: workload_sims(n, rank)  # noqa: E731
+    else:
+        model = abi.GELIO_MODEL_1D_BP if args.workload == "bp" else abi.GELIO_MODEL_1D_FP
+        metric = ("1D B-p" if args.workload == "bp" else "1D F-p") + " trajectories/s"
+        config = {"workload": workload_1d.__doc__.split(";")[0 if args.workload == "bp" else 1].strip(),
+                  "model": metric[:6], "particles": args.particles,
+                  "l2": "flushed between timed steps (256 MiB write)"}
+        make = lambda n: workload_1d(model, n, rank)  # noqa: E731
+    sims = make(args.particles)
     n = len(sims)
     total_traj = sum(s.n_particles for s in sims)
     tune = None
     if not args.no_tune:
         # the production batch with fewer particles per simulation
-        tune = eng.autotune(workload_sims(max(1, min(args.particles, 1_000_000)), rank))
+        tune = eng.autotune(make(max(1, min(args.particles, 1_000_000))))
 
     # device-resident inputs for `value`
     raw = bytes((abi.SimParams * n)(*sims))
@@ -293,6 +502,29 @@ def main():
         if world > 1:
             import torch.distributed as dist
             dist.destroy_process_group()
+        return
+
+    if not headline:
+        # the same workload with FP64 steps (B-p: the FP64-step variant)
+        fp64 = None
+        if args.workload == "bp":
+            eng.run(sims, precision=abi.GELIO_PREC_FP64)
+            t0 = time.perf_counter()
+            r64 = eng.run(sims, precision=abi.GELIO_PREC_FP64)
+            fp64 = {"value": total_traj / (time.perf_counter() - t0), "unit": "trajectories/s",
+                    "kernel_ms": r64.stats.kernel_ms}
+        line = {"metric": metric, "value": value, "unit": "trajectories/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t_rank / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": dict(config, tuned={"block": tune.block_size, "refill": tune.refill_interval}
+                               if tune else None),
+                "particle_steps_per_s": steps_per_run / (statistics.mean(kernel_ms) / 1e3),
+                "e2e": {"value": e2e_value, "unit": "trajectories/s",
+                        "h2d_bytes_per_step": n * ctypes.sizeof(abi.SimParams),
+                        "d2h_bytes_per_step": n * ctypes.sizeof(abi.Spectra)},
+                "gpu_launches": 3 * args.steps, "fp64_steps": fp64, "clocks": clk.summary()}
+        print(json.dumps(line), flush=True)
+        eng.close()
         return
 
     fp32_tflops, xu_gops = eng.measure_peaks()

@@ -115,12 +115,24 @@ class Trajectory(Structure):
     ]
 
 
+class SurrogateOpts(Structure):
+    _fields_ = [
+        ("members", c_int32), ("batch_rows", c_int32), ("lis", c_int32), ("min_count", c_int32),
+        ("lr", c_float), ("lr_final", c_float), ("fallback_std", c_float), ("t_min", c_float),
+        ("t_max", c_float), ("reserved0", c_int32), ("seed", c_uint64), ("reserved", c_int32 * 8),
+    ]
+
+
+GELIO_SURR_FEATURES = 7
+GELIO_SURR_PARAMS = 199681
+
 assert ctypes.sizeof(SimParams) == 96
 assert ctypes.sizeof(Spectra) == 64808
 assert ctypes.sizeof(ExitRecord) == 32
 assert ctypes.sizeof(RunOpts) == 64
 assert ctypes.sizeof(RunStats) == 88
 assert ctypes.sizeof(Trajectory) == 40
+assert ctypes.sizeof(SurrogateOpts) == 80
 
 # C-ABI entry points declared in include/gelio.h: name -> (restype, argtypes)
 PROTOTYPES = {
@@ -140,6 +152,23 @@ PROTOTYPES = {
     "gelio_autotune": (c_int32, [c_void_p, POINTER(SimParams), c_int32, POINTER(RunOpts)]),
     "gelio_measure_peaks": (c_int32, [c_void_p, POINTER(c_double), POINTER(c_double)]),
     "gelio_run_noalloc": (c_int32, [c_void_p, c_int32, POINTER(RunOpts), c_void_p, c_void_p]),
+    "gelio_surrogate_create": (c_int32, [c_void_p, POINTER(SurrogateOpts), POINTER(c_void_p)]),
+    "gelio_surrogate_destroy": (None, [c_void_p]),
+    "gelio_surrogate_features": (c_int32, [POINTER(SimParams), c_double, POINTER(c_float)]),
+    "gelio_surrogate_add_spectra": (c_int32, [c_void_p, POINTER(SimParams), POINTER(Spectra), c_int32,
+                                              POINTER(c_int64)]),
+    "gelio_surrogate_add_rows": (c_int32, [c_void_p, POINTER(c_float), POINTER(c_float), c_int64,
+                                           POINTER(c_int64)]),
+    "gelio_surrogate_train": (c_int32, [c_void_p, c_int32, POINTER(c_float)]),
+    "gelio_surrogate_predict": (c_int32, [c_void_p, POINTER(SimParams), c_int32, POINTER(c_double),
+                                          POINTER(c_double)]),
+    "gelio_surrogate_spectra": (c_int32, [c_void_p, POINTER(SimParams), c_int32, POINTER(RunOpts),
+                                          POINTER(c_double), POINTER(c_double), POINTER(c_int32)]),
+    "gelio_surrogate_get_params": (c_int32, [c_void_p, c_int32, POINTER(c_float)]),
+    "gelio_surrogate_set_params": (c_int32, [c_void_p, c_int32, POINTER(c_float)]),
+    "gelio_surrogate_forward": (c_int32, [c_void_p, c_int32, POINTER(c_float), c_int32, POINTER(c_float)]),
+    "gelio_surrogate_gradient": (c_int32, [c_void_p, c_int32, POINTER(c_float), POINTER(c_float), c_int32,
+                                           POINTER(c_float), POINTER(c_float)]),
 }
 
 _LIB = None

@@ -1,7 +1,7 @@
 """In-tree build of libgelio_cuda.so for sm_103a (nvcc, no cmake).
 
-The five translation units (four model kernels + the C-ABI host code) are
-compiled in parallel and linked into geliosphere_gb300/_lib/libgelio_cuda.so.
+The translation units (four model kernels, the C-ABI host code, the
+allocation-free entry point and the surrogate network) are compiled in parallel and linked into geliosphere_gb300/_lib/libgelio_cuda.so.
 """
 from __future__ import annotations
 
@@ -17,7 +17,7 @@ OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB = os.path.join(OUT_DIR, "libgelio_cuda.so")
 
-UNITS = ["api.cu", "k_fp.cu", "k_bp.cu", "k_solarprop.cu", "k_geliosphere.cu", "noalloc.cu"]
+UNITS = ["api.cu", "k_fp.cu", "k_bp.cu", "k_solarprop.cu", "k_geliosphere.cu", "noalloc.cu", "mlp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # FP32 SDE steps: flush denormals, approximate division/sqrt where the
 # kernels ask for them; the bit-exact parts use explicit _rn intrinsics.

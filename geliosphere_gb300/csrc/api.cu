@@ -919,6 +919,13 @@ int32_t gelio_measure_peaks(gelio_ctx *c, double *fp32_tflops, double *xu_gops) 
   return GELIO_OK;
 }
 
+}  // extern "C"
+
+// Device of a context, for the surrogate built on it.
+int gelio_internal_device(const gelio_ctx *c) { return c ? c->device : 0; }
+
+extern "C" {
+
 int32_t gelio_autotune(gelio_ctx *c, const gelio_sim_params *sims, int32_t n, gelio_run_opts *best) {
   if (!c || !sims || n < 1 || n > kMaxSims) return GELIO_ERR_INVALID_ARGUMENT;
   int rc;

@@ -1,0 +1,380 @@
+// Kernels of the spectrum surrogate: a 7 -> 256 -> 256 -> 256 -> 256 -> 1
+// MLP with SiLU, BF16 weights and activations, FP32 accumulation.
+//
+// Every layer product is one tcgen05 GEMM of the form C[M x N] = A[M x K] *
+// B[N x K]^T with both operands K-major in HBM (row-major, K contiguous):
+//   forward   Z_l   = X_{l-1} W_l^T          A = X_{l-1} [rows x in], B = W_l   [256 x in]
+//   input grad dX   = dH_l W_l               A = dH_l    [rows x 256], B = W_l^T [in x 256]
+//   weight grad dW_l = dH_l^T X_{l-1}        A = dH_l^T  [256 x rows], B = X_{l-1}^T [in x rows]
+// so every layer writes its activations / gradients twice, row-major and
+// transposed, from the GEMM epilogue that produces them.  The epilogues are
+// fused: bias + SiLU (+ the 256 -> 1 head on the last hidden layer) going
+// forward, SiLU' of the stored pre-activation going back; weight gradients
+// are split over the batch (split-K) into FP32 partials reduced in a fixed
+// order, so a gradient is deterministic.
+#pragma once
+#include <cuda_bf16.h>
+
+#include "tc_sm103.cuh"
+
+namespace gelio {
+namespace mlp {
+
+constexpr int kWidth = 256;       // hidden width
+constexpr int kFeatures = 7;      // (K0, V, tilt, polarity, r, theta, log T)
+constexpr int kInPad = 64;        // first-layer K padded to one 128-byte row
+constexpr int kTileM = 128;       // GEMM rows per tile (TMEM lanes)
+constexpr int kChunk = 64;        // K per pipeline stage (128 B of BF16)
+constexpr int kStages = 4;
+constexpr int kThreads = 128;
+constexpr uint32_t kStageA = kTileM * kChunk * 2;   // 16 KiB
+constexpr uint32_t kStageB = kWidth * kChunk * 2;   // 32 KiB (N = 256)
+constexpr uint32_t kTmemCols = 256;
+constexpr size_t kGemmSmem = 1024 + (size_t)kStages * (kStageA + kStageB) + 128;
+
+// Flat parameter layout (FP32 master copy and gradients).
+constexpr int kOffW1 = 0;                                   // [256][7]
+constexpr int kOffB1 = kOffW1 + kWidth * kFeatures;         // [256]
+constexpr int kOffW2 = kOffB1 + kWidth;                     // [256][256]
+constexpr int kOffB2 = kOffW2 + kWidth * kWidth;
+constexpr int kOffW3 = kOffB2 + kWidth;
+constexpr int kOffB3 = kOffW3 + kWidth * kWidth;
+constexpr int kOffW4 = kOffB3 + kWidth;
+constexpr int kOffB4 = kOffW4 + kWidth * kWidth;
+constexpr int kOffW5 = kOffB4 + kWidth;                     // [256]
+constexpr int kOffB5 = kOffW5 + kWidth;                     // [1]
+constexpr int kParams = kOffB5 + 1;                         // 199,681
+
+enum Mode { FWD = 0, FWD_LAST = 1, INFER = 2, INFER_LAST = 3, DX = 4, DW = 5 };
+
+struct GemmArgs {
+  int M;                  // GEMM rows: batch rows (FWD*, INFER*, DX) or 256 output features (DW)
+  int N;                  // GEMM columns: 256, or 64 for the first layer's DW
+  int K;                  // reduction length: layer fan-in, or batch rows (DW)
+  int k_per_split;        // DW: batch rows per split (multiple of 64); else K
+  int splits;             // DW: number of splits; else 1
+  int ldt;                // row count of the transposed outputs (batch rows)
+  const float *bias;      // FWD*, INFER*: [256]
+  const float *w5;        // *_LAST: head weights [256]
+  const float *b5;        // *_LAST: head bias [1]
+  __nv_bfloat16 *z_out;   // FWD*: pre-activations [M][256]
+  __nv_bfloat16 *x_out;   // FWD, INFER: activations [M][256]
+  __nv_bfloat16 *xt_out;  // FWD*: activations transposed [256][ldt]
+  float *y_out;           // *_LAST: head outputs [M]
+  const __nv_bfloat16 *z_prev;   // DX: pre-activations of the layer below [M][256]
+  __nv_bfloat16 *dh_out;  // DX: [M][256]
+  __nv_bfloat16 *dht_out; // DX: [256][ldt]
+  float *partial;         // DW: [splits][N][256]
+  unsigned *error;        // set nonzero when a wait times out
+  unsigned long long timeout_ns;
+};
+
+__device__ __forceinline__ float silu_f(float z) { return z / (1.0f + __expf(-z)); }
+__device__ __forceinline__ float silu_grad_f(float z) {
+  const float s = 1.0f / (1.0f + __expf(-z));
+  return s * (1.0f + z * (1.0f - s));
+}
+
+template <int MODE>
+__device__ __forceinline__ void gemm_epilogue(const GemmArgs &a, int row, uint32_t trow, int split) {
+  const bool valid = row < a.M;
+  float ysum = 0.0f;
+  const int nchunks = a.N / 32;
+  for (int c = 0; c < nchunks; ++c) {
+    float v[32];
+    tc::tmem_ld32(trow + (uint32_t)(c * 32), v);     // warp-wide: every lane executes it
+    const int n0 = c * 32;
+    if constexpr (MODE == DW) {
+      float *p = a.partial + ((size_t)split * a.N + n0) * kWidth + row;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) p[(size_t)j * kWidth] = v[j];
+      continue;
+    }
+    if (!valid) continue;
+    __align__(16) __nv_bfloat16 out[32];
+    if constexpr (MODE == DX) {
+      __align__(16) __nv_bfloat16 zp[32];
+      const uint4 *src = reinterpret_cast<const uint4 *>(a.z_prev + (size_t)row * kWidth + n0);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) reinterpret_cast<uint4 *>(zp)[q] = src[q];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) out[j] = __float2bfloat16_rn(v[j] * silu_grad_f(__bfloat162float(zp[j])));
+      uint4 *dst = reinterpret_cast<uint4 *>(a.dh_out + (size_t)row * kWidth + n0);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) dst[q] = reinterpret_cast<uint4 *>(out)[q];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) a.dht_out[(size_t)(n0 + j) * a.ldt + row] = out[j];
+    } else {
+    // forward family
+    __align__(16) __nv_bfloat16 zb[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      const float z = v[j] + __ldg(a.bias + n0 + j);
+      zb[j] = __float2bfloat16_rn(z);
+      out[j] = __float2bfloat16_rn(silu_f(z));
+      if (MODE == FWD_LAST || MODE == INFER_LAST) ysum += __bfloat162float(out[j]) * __ldg(a.w5 + n0 + j);
+    }
+    if (MODE == FWD || MODE == FWD_LAST) {
+      uint4 *dz = reinterpret_cast<uint4 *>(a.z_out + (size_t)row * kWidth + n0);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) dz[q] = reinterpret_cast<uint4 *>(zb)[q];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) a.xt_out[(size_t)(n0 + j) * a.ldt + row] = out[j];
+    }
+    if (MODE == FWD || MODE == INFER) {
+      uint4 *dx = reinterpret_cast<uint4 *>(a.x_out + (size_t)row * kWidth + n0);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) dx[q] = reinterpret_cast<uint4 *>(out)[q];
+    }
+    }
+  }
+  if ((MODE == FWD_LAST || MODE == INFER_LAST) && valid) a.y_out[row] = ysum + __ldg(a.b5);
+}
+
+// One CTA per SM (the 4-stage ring takes 192 KiB of shared memory), tiles of
+// 128 GEMM rows handed out round-robin.  Thread 0 issues the TMA loads (up
+// to kStages chunks ahead) and the MMAs; all four warps run the epilogue,
+// warp w reading TMEM lanes 32w..32w+31 (one GEMM row per thread).
+template <int MODE>
+__global__ void __launch_bounds__(kThreads, 1)
+    k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const GemmArgs a) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ int s_abort;
+  const uint32_t s0 = tc::smem_u32(smem_raw);
+  unsigned char *base = smem_raw + ((1024u - (s0 & 1023u)) & 1023u);
+  unsigned char *stA = base;
+  unsigned char *stB = base + kStages * kStageA;
+  uint64_t *full = reinterpret_cast<uint64_t *>(stB + kStages * kStageB);
+  uint64_t *empty = full + kStages;
+  uint64_t *accum = empty + kStages;
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(accum + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t bytesB = (uint32_t)a.N * kChunk * 2;
+  const uint32_t idesc = tc::idesc_bf16_f32(kTileM, a.N);
+
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    tc::mbar_init(accum, 1);
+    tc::fence_mbar_init();
+    tc::tma_prefetch(&tmA);
+    tc::tma_prefetch(&tmB);
+    s_abort = 0;
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tslot, kTmemCols);
+    tc::tmem_relinquish();
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = *tslot;
+  const unsigned long long deadline = tc::now_ns() + a.timeout_ns;
+
+  const int m_tiles = (a.M + kTileM - 1) / kTileM;
+  const int tiles = m_tiles * a.splits;
+  uint32_t load_it = 0, mma_it = 0, acc_phase = 0;
+  for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
+    const int tm = t % m_tiles;
+    const int split = t / m_tiles;
+    const int k0 = split * a.k_per_split;
+    const int klen = min(a.k_per_split, a.K - k0);
+    const int nk = (klen + kChunk - 1) / kChunk;
+    if (nk <= 0) continue;
+    if (tid == 0 && !s_abort) {
+      bool ok = true;
+      int issued = 0;
+      for (int kc = 0; kc < nk && ok; ++kc) {
+        while (issued < nk && load_it < mma_it + kStages) {
+          const uint32_t st = load_it % kStages;
+          if (load_it >= (uint32_t)kStages && !tc::mbar_wait(&empty[st], ((load_it / kStages) - 1) & 1, deadline)) {
+            ok = false;
+            break;
+          }
+          tc::mbar_expect_tx(&full[st], kStageA + bytesB);
+          tc::tma_load_2d(stA + st * kStageA, &tmA, k0 + issued * kChunk, tm * kTileM, &full[st]);
+          tc::tma_load_2d(stB + st * kStageB, &tmB, k0 + issued * kChunk, 0, &full[st]);
+          ++load_it;
+          ++issued;
+        }
+        if (!ok) break;
+        const uint32_t st = mma_it % kStages;
+        if (!tc::mbar_wait(&full[st], (mma_it / kStages) & 1, deadline)) {
+          ok = false;
+          break;
+        }
+        tc::tc_fence_after();
+        const uint32_t aa = tc::smem_u32(stA + st * kStageA), bb = tc::smem_u32(stB + st * kStageB);
+#pragma unroll
+        for (int k = 0; k < kChunk / 16; ++k)
+          tc::mma_bf16(tmem, tc::sdesc_sw128(aa + k * 32), tc::sdesc_sw128(bb + k * 32), idesc,
+                       (kc > 0 || k > 0) ? 1u : 0u);
+        tc::mma_commit(&empty[st]);
+        ++mma_it;
+      }
+      if (ok) {
+        tc::mma_commit(accum);
+      } else {
+        s_abort = 1;
+        atomicExch(a.error, 1u);
+        // let the copies and products already in flight land before the
+        // shared memory and TMEM are given back (bounded again)
+        const unsigned long long d2 = tc::now_ns() + 1000000000ull;
+        for (uint32_t it = mma_it; it < load_it; ++it) tc::mbar_wait(&full[it % kStages], (it / kStages) & 1, d2);
+        if (mma_it > 0) tc::mbar_wait(&empty[(mma_it - 1) % kStages], ((mma_it - 1) / kStages) & 1, d2);
+      }
+    }
+    __syncwarp();
+    if (!s_abort && !tc::mbar_wait(accum, acc_phase & 1, deadline)) {
+      s_abort = 1;
+      atomicExch(a.error, 2u);
+    }
+    ++acc_phase;
+    __syncthreads();
+    if (s_abort) break;
+    tc::tc_fence_after();
+    gemm_epilogue<MODE>(a, tm * kTileM + warp * 32 + lane, tmem + ((uint32_t)(warp * 32) << 16), split);
+    tc::tc_fence_before();
+    __syncthreads();
+  }
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
+}
+
+// ----------------------------------------------------------------------------
+// CUDA-core kernels around the GEMMs
+// ----------------------------------------------------------------------------
+
+// Batch rows order[offset .. offset + rows) of the training set (past
+// n_order: padding rows of zeros).  Writes X0 [rows][64] (features in
+// columns 0..6; the padding columns stay zero from allocation), X0^T
+// [64][rows] (rows 0..6) and the targets.
+__global__ void k_gather(const float *__restrict__ feats, const float *__restrict__ targ,
+                         const int *__restrict__ order, long long n_order, long long offset, int rows,
+                         __nv_bfloat16 *__restrict__ x0, __nv_bfloat16 *__restrict__ x0t, float *__restrict__ y) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= rows) return;
+  const long long k = offset + m;
+  const int src = (k < n_order) ? order[k] : -1;
+#pragma unroll
+  for (int f = 0; f < kFeatures; ++f) {
+    const __nv_bfloat16 v = __float2bfloat16_rn(src >= 0 ? feats[(size_t)src * kFeatures + f] : 0.0f);
+    x0[(size_t)m * kInPad + f] = v;
+    x0t[(size_t)f * rows + m] = v;
+  }
+  if (y) y[m] = (src >= 0 && targ) ? targ[src] : 0.0f;
+}
+
+// Loss and the head's backward pass: dy = 2 (yhat - y) / n for the first n
+// rows (0 for padding), dH4 = dy * w5 * SiLU'(Z4) in both layouts, and one
+// squared-error partial per block.
+__global__ void k_head_backward(const float *__restrict__ yhat, const float *__restrict__ y, int n_valid, int rows,
+                                const float *__restrict__ w5, const __nv_bfloat16 *__restrict__ z4,
+                                __nv_bfloat16 *__restrict__ dh4, __nv_bfloat16 *__restrict__ dh4t,
+                                float *__restrict__ dy, float *__restrict__ loss_part) {
+  __shared__ float red[kThreads];
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  float se = 0.0f;
+  if (m < rows) {
+    const float e = (m < n_valid) ? (yhat[m] - y[m]) : 0.0f;
+    se = e * e;
+    const float d = 2.0f * e / (float)n_valid;
+    dy[m] = d;
+    for (int n = 0; n < kWidth; ++n) {
+      const float g = d * __ldg(w5 + n) * silu_grad_f(__bfloat162float(z4[(size_t)m * kWidth + n]));
+      const __nv_bfloat16 b = __float2bfloat16_rn(g);
+      dh4[(size_t)m * kWidth + n] = b;
+      dh4t[(size_t)n * rows + m] = b;
+    }
+  }
+  red[threadIdx.x] = se;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) loss_part[blockIdx.x] = red[0];
+}
+
+// out[r] = sum_c src[r][c] * (w ? w[c] : 1), one block per row, fixed order.
+__global__ void k_rowsum_bf16(const __nv_bfloat16 *__restrict__ src, int cols, const float *__restrict__ w,
+                              float *__restrict__ out) {
+  __shared__ float red[256];
+  const __nv_bfloat16 *row = src + (size_t)blockIdx.x * cols;
+  float s = 0.0f;
+  for (int c = threadIdx.x; c < cols; c += blockDim.x) s += __bfloat162float(row[c]) * (w ? w[c] : 1.0f);
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+    if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = red[0];
+}
+
+__global__ void k_sum_f32(const float *__restrict__ src, int n, float *__restrict__ out) {
+  __shared__ float red[256];
+  float s = 0.0f;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += src[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+    if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
+}
+
+// dW[o][i] (i < fan_in) = sum over splits of partial[s][i][o].
+__global__ void k_reduce_dw(const float *__restrict__ partial, int splits, int n_cols, int fan_in,
+                            float *__restrict__ dw) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= kWidth * fan_in) return;
+  const int o = idx / fan_in, i = idx % fan_in;
+  float s = 0.0f;
+  for (int k = 0; k < splits; ++k) s += partial[((size_t)k * n_cols + i) * kWidth + o];
+  dw[idx] = s;
+}
+
+// Adam (bias-corrected) on the FP32 master parameters.
+__global__ void k_adam(float *__restrict__ p, const float *__restrict__ g, float *__restrict__ m1,
+                       float *__restrict__ m2, int n, float lr, float b1, float b2, float eps, float c1, float c2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float a = b1 * m1[i] + (1.0f - b1) * gi;
+  const float b = b2 * m2[i] + (1.0f - b2) * gi * gi;
+  m1[i] = a;
+  m2[i] = b;
+  p[i] -= lr * (a / c1) / (sqrtf(b / c2) + eps);
+}
+
+// BF16 operand copies of the master weights: W1 padded to [256][64], W2..W4
+// and their transposes.
+__global__ void k_pack(const float *__restrict__ p, __nv_bfloat16 *__restrict__ w1, __nv_bfloat16 *__restrict__ w2,
+                       __nv_bfloat16 *__restrict__ w3, __nv_bfloat16 *__restrict__ w4, __nv_bfloat16 *__restrict__ w2t,
+                       __nv_bfloat16 *__restrict__ w3t, __nv_bfloat16 *__restrict__ w4t) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx < kWidth * kInPad) {
+    const int o = idx / kInPad, i = idx % kInPad;
+    w1[idx] = __float2bfloat16_rn(i < kFeatures ? p[kOffW1 + o * kFeatures + i] : 0.0f);
+  }
+  if (idx < kWidth * kWidth) {
+    const int o = idx / kWidth, i = idx % kWidth;
+    const __nv_bfloat16 a = __float2bfloat16_rn(p[kOffW2 + idx]);
+    const __nv_bfloat16 b = __float2bfloat16_rn(p[kOffW3 + idx]);
+    const __nv_bfloat16 c = __float2bfloat16_rn(p[kOffW4 + idx]);
+    w2[idx] = a;
+    w3[idx] = b;
+    w4[idx] = c;
+    w2t[i * kWidth + o] = a;
+    w3t[i * kWidth + o] = b;
+    w4t[i * kWidth + o] = c;
+  }
+}
+
+}  // namespace mlp
+}  // namespace gelio

@@ -256,3 +256,18 @@ def round_g(rows: np.ndarray) -> np.ndarray:
     """printf("%g") -> strtod of every value (the log.dat text round trip)."""
     flat = [float("%g" % x) for x in np.asarray(rows, dtype=np.float64).ravel()]
     return np.array(flat, dtype=np.float64).reshape(np.shape(rows))
+
+
+def lis_values(which: int, T):
+    """Local interstellar spectra of the 2D evaluator (TwoDimensionBpResults.cpp:50-60):
+    0 Weber, 1 Usoskin 2005, 2 Burger; T in GeV."""
+    T = np.asarray(T, dtype=np.float64)
+    lt = np.log(T)
+    if which == 0:
+        return 21.1 * np.exp(-2.8 * lt) / (1.0 + 5.85 * np.exp(-1.22 * lt) + 1.18 * np.exp(-2.54 * lt))
+    if which == 1:
+        tt = T + 0.938
+        beta = np.sqrt(T * (tt + 0.938)) / tt
+        return 2.7e3 * np.exp(1.12 * lt) * np.exp(-3.93 * np.log((T + 0.67) / 1.67)) / (beta * beta)
+    p = np.sqrt(T * T + 2.0 * T * 0.938)
+    return 1.9e4 * np.exp(-2.78 * np.log(p)) / (1.0 + 0.4866 * np.exp(-2.51 * np.log(p)))

@@ -321,6 +321,87 @@ int32_t gelio_run_noalloc(const gelio_sim_params *d_sims, int32_t n_sims,
  * no reference counterpart. */
 int32_t gelio_measure_peaks(gelio_ctx *ctx, double *fp32_tflops, double *xu_gops);
 
+/* ------------------------------------------------------------------------
+ * Spectrum surrogate (no reference counterpart: a learned addition on top
+ * of the reference's Monte Carlo method).
+ *
+ * An ensemble of MLPs 7 -> 256 -> 256 -> 256 -> 256 -> 1 (SiLU, BF16
+ * weights and activations, FP32 accumulation) maps a 2D Geliosphere
+ * simulation's (K0, V, tilt, polarity, r_injection, theta_injection) and a
+ * 1 AU kinetic energy T to ln(J_mod(T) / J_LIS(T)).  It is trained on the
+ * GPU, by this library's own forward and backward kernels (tcgen05 GEMMs),
+ * on spectra this library's Monte Carlo produced, and falls back to the
+ * Monte Carlo where the members disagree.
+ * ------------------------------------------------------------------------ */
+typedef struct gelio_surrogate gelio_surrogate;
+
+#define GELIO_SURR_FEATURES 7
+#define GELIO_SURR_PARAMS 199681   /* FP32 parameters of one member (flat layout below) */
+/* Flat layout: W1 [256][7], b1 [256], W2 [256][256], b2, W3, b3, W4, b4,
+ * w5 [256], b5 [1]; W_l[o][i] multiplies input i into output o. */
+
+typedef struct gelio_surrogate_opts {
+    int32_t members;        /* ensemble size (0: 5) */
+    int32_t batch_rows;     /* training batch rows, a multiple of 256 (0: 16384) */
+    int32_t lis;            /* LIS of the target ratio: 0 Weber, 1 Usoskin 2005, 2 Burger */
+    int32_t min_count;      /* grid points with fewer exits are not trained on (0: 64) */
+    float lr;               /* Adam learning rate, cosine-decayed ... (0: 2e-3) */
+    float lr_final;         /* ... to this over the run (0: 2e-5) */
+    float fallback_std;     /* ensemble std of ln ratio above which the MC runs (0: 0.03) */
+    float t_min, t_max;     /* energy range [GeV] that std is tested over (0: 0.1, 10) */
+    int32_t reserved0;
+    uint64_t seed;          /* initial weights and shuffling */
+    int32_t reserved[8];
+} gelio_surrogate_opts;
+
+int32_t gelio_surrogate_create(gelio_ctx *ctx, const gelio_surrogate_opts *opts, gelio_surrogate **out);
+void gelio_surrogate_destroy(gelio_surrogate *s);
+
+/* Normalised network input of one (simulation, energy [GeV]). */
+int32_t gelio_surrogate_features(const gelio_sim_params *sim, double t_gev, float out[7]);
+
+/* Training rows from Monte Carlo spectra: every 2D Geliosphere simulation
+ * run with GELIO_INJ_LOG_GRID (grid_bins = 0) contributes, for each grid
+ * point j with at least min_count exits, features(sim, T_j) and
+ * ln((grid_w[lis][j] / grid_n[j]) / J_LIS(T_j)).  *n_rows: rows held. */
+int32_t gelio_surrogate_add_spectra(gelio_surrogate *s, const gelio_sim_params *sims,
+                                    const gelio_spectra *spectra, int32_t n, int64_t *n_rows);
+
+/* Training rows given directly: normalised inputs x [n][7], targets t [n]. */
+int32_t gelio_surrogate_add_rows(gelio_surrogate *s, const float *x, const float *t, int64_t n,
+                                 int64_t *n_rows);
+
+/* `epochs` passes of Adam over the held rows for every member (MSE on the
+ * ln ratio); last_loss[members] receives each member's last-epoch loss. */
+int32_t gelio_surrogate_train(gelio_surrogate *s, int32_t epochs, float *last_loss);
+
+/* Ensemble mean and standard deviation of ln(J_mod / J_LIS) at each
+ * GELIO_INJ_LOG_GRID point of each simulation; outputs hold the points of
+ * sims[0], then sims[1], ... (sum of inj_points entries). */
+int32_t gelio_surrogate_predict(gelio_surrogate *s, const gelio_sim_params *sims, int32_t n,
+                                double *ln_ratio, double *ln_std);
+
+/* predict, then run the Monte Carlo (gelio_run with mc_opts, the sims'
+ * own particle counts) for every simulation whose largest std over
+ * [t_min, t_max] exceeds fallback_std and return its ratio there
+ * (ln_std = 0, used_mc[i] = 1). */
+int32_t gelio_surrogate_spectra(gelio_surrogate *s, const gelio_sim_params *sims, int32_t n,
+                                const gelio_run_opts *mc_opts, double *ln_ratio, double *ln_std,
+                                int32_t *used_mc);
+
+/* Member m's FP32 parameters (GELIO_SURR_PARAMS floats), for persistence
+ * and checks; set_params also clears that member's Adam state. */
+int32_t gelio_surrogate_get_params(gelio_surrogate *s, int32_t member, float *params);
+int32_t gelio_surrogate_set_params(gelio_surrogate *s, int32_t member, const float *params);
+
+/* One forward pass of member m on normalised inputs x [n][7] -> y [n]. */
+int32_t gelio_surrogate_forward(gelio_surrogate *s, int32_t member, const float *x, int32_t n, float *y);
+
+/* Mean squared error and its gradient (GELIO_SURR_PARAMS floats) for member
+ * m on x [n][7] and targets t [n], n <= batch_rows; no update. */
+int32_t gelio_surrogate_gradient(gelio_surrogate *s, int32_t member, const float *x, const float *t,
+                                 int32_t n, float *loss, float *grad);
+
 #ifdef __cplusplus
 }
 #endif

@@ -78,6 +78,13 @@ def load():
     lib.gor_cpu_baseline.argtypes = [c_int, POINTER(CpuParams), c_int, c_int, c_uint32,
                                      POINTER(c_int64), POINTER(c_int64), POINTER(c_int64)]
     lib.gor_cpu_baseline.restype = c_double
+    F32P, F64P = POINTER(c_float), POINTER(c_double)
+    lib.gor_mlp_params.argtypes = []
+    lib.gor_mlp_params.restype = c_int
+    lib.gor_mlp_forward.argtypes = [F32P, F32P, c_int, F64P]
+    lib.gor_mlp_forward.restype = None
+    lib.gor_mlp_grad.argtypes = [F32P, F32P, F32P, c_int, F64P, F64P]
+    lib.gor_mlp_grad.restype = None
     _LIB = lib
     return lib
 
@@ -146,3 +153,29 @@ def cpu_params_from_dict(d: dict) -> CpuParams:
     for k, _ in CpuParams._fields_:
         setattr(p, k, int(d[k]) if k == "useUniformInjection" else float(d[k]))
     return p
+
+
+def mlp_forward(params: np.ndarray, x: np.ndarray) -> np.ndarray:
+    """Surrogate network forward of the CPU restatement (BF16 storage points
+    emulated, FP64 arithmetic)."""
+    lib = load()
+    p = np.ascontiguousarray(params, np.float32)
+    x = np.ascontiguousarray(x, np.float32).reshape(-1, 7)
+    y = np.zeros(x.shape[0])
+    lib.gor_mlp_forward(p.ctypes.data_as(POINTER(c_float)), x.ctypes.data_as(POINTER(c_float)), x.shape[0],
+                        y.ctypes.data_as(POINTER(c_double)))
+    return y
+
+
+def mlp_grad(params: np.ndarray, x: np.ndarray, t: np.ndarray):
+    """Mean squared error and its gradient, CPU restatement."""
+    lib = load()
+    p = np.ascontiguousarray(params, np.float32)
+    x = np.ascontiguousarray(x, np.float32).reshape(-1, 7)
+    t = np.ascontiguousarray(t, np.float32)
+    g = np.zeros(lib.gor_mlp_params())
+    loss = c_double()
+    lib.gor_mlp_grad(p.ctypes.data_as(POINTER(c_float)), x.ctypes.data_as(POINTER(c_float)),
+                     t.ctypes.data_as(POINTER(c_float)), x.shape[0], ctypes.byref(loss),
+                     g.ctypes.data_as(POINTER(c_double)))
+    return loss.value, g

@@ -42,14 +42,15 @@ def test_struct_layouts_match_header(tmp_path):
     from geliosphere_gb300 import abi
     prog = tmp_path / "sz.c"
     prog.write_text('#include <stdio.h>\n#include "gelio.h"\n'
-                    'int main(){printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(gelio_sim_params), '
+                    'int main(){printf("%zu %zu %zu %zu %zu %zu %zu\\n", sizeof(gelio_sim_params), '
                     'sizeof(gelio_spectra), sizeof(gelio_exit_record), sizeof(gelio_run_opts), '
-                    'sizeof(gelio_run_stats), sizeof(gelio_trajectory));}\n')
+                    'sizeof(gelio_run_stats), sizeof(gelio_trajectory), sizeof(gelio_surrogate_opts));}\n')
     exe = tmp_path / "sz"
     subprocess.run(["gcc", "-I" + os.path.join(ROOT, "include"), str(prog), "-o", str(exe)], check=True)
     sizes = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
     assert sizes == [ctypes.sizeof(abi.SimParams), ctypes.sizeof(abi.Spectra), ctypes.sizeof(abi.ExitRecord),
-                     ctypes.sizeof(abi.RunOpts), ctypes.sizeof(abi.RunStats), ctypes.sizeof(abi.Trajectory)]
+                     ctypes.sizeof(abi.RunOpts), ctypes.sizeof(abi.RunStats), ctypes.sizeof(abi.Trajectory),
+                     ctypes.sizeof(abi.SurrogateOpts)]
 
 
 def test_status_strings_and_null_arguments(lib):

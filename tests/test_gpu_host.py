@@ -85,15 +85,28 @@ def test_cli_run_then_evaluate_identical(exe, tmp_path, flag, model_dir, files):
     for f in files + ["log.dat", "simulation_log.txt"]:
         assert (out / f).exists(), f"{f} missing: {err}"
     assert "Model:" in (out / "simulation_log.txt").read_text()
-    # evaluation-only mode re-bins the written log: same files, byte for byte,
-    # and the input log stays where it is
+    # evaluation-only mode reads countLines() - 1 records, as the reference
+    # does (TwoDimensionBpResults.cpp:21): with the last line doubled it
+    # re-bins every exit of the run and reproduces the fused spectra
+    padded = tmp_path / "padded.dat"
+    lines = (out / "log.dat").read_text().splitlines(keepends=True)
+    padded.write_text("".join(lines + lines[-1:]))
     ev = tmp_path / "ev"
     ev.mkdir()
-    rc, err = run(exe, [flag, "--evaluation", str(out / "log.dat")], ev)
+    rc, err = run(exe, [flag, "--evaluation", str(padded)], ev)
     assert rc == 0, err
     for f in files:
         same_table(ev / f, out / f, f)
-    assert (out / "log.dat").exists()
+    # on the log as written, exactly the last record is left out
+    ev1 = tmp_path / "ev1"
+    ev1.mkdir()
+    rc, err = run(exe, [flag, "--evaluation", str(out / "log.dat")], ev1)
+    assert rc == 0, err
+    assert (out / "log.dat").exists()   # the evaluated log is never unlinked
+    if files is SPECTRA_2D:
+        n_all = np.loadtxt(out / "Ams.dat")[:, 3].sum()
+        n_ev = np.loadtxt(ev1 / "Ams.dat")[:, 3].sum()
+        assert n_ev in (n_all, n_all - 1)
 
 
 def test_cli_removes_log_by_default(exe, tmp_path):

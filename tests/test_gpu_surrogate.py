@@ -1,0 +1,100 @@
+"""The surrogate network's GPU kernels (tcgen05 GEMMs with fused epilogues)
+against the CPU restatement: forward outputs and every parameter gradient;
+then training on the GPU and the fallback to the Monte Carlo."""
+import numpy as np
+import pytest
+
+from geliosphere_gb300 import abi, make_sim
+from geliosphere_gb300 import surrogate as sg
+from test_surrogate_oracle import data, init_params
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def sur(engine):
+    s = sg.Surrogate(engine, members=2, batch_rows=4096, seed=3)
+    yield s
+    s.close()
+
+
+def test_forward_matches_oracle(sur, oracle):
+    p = init_params(seed=11)
+    sur.set_params(0, p)
+    x, _ = data(9000, seed=2)        # more than two batches, ragged tail
+    y = sur.forward(0, x)
+    ref = oracle.mlp_forward(p, x)
+    err = np.abs(y - ref)
+    # BF16 activations: the two sides round the same values, rare 1-ulp flips
+    assert np.median(err) < 2e-3 * np.abs(ref).max()
+    assert err.max() < 3e-2 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("n", [4096, 3001, 130])
+def test_gradient_matches_oracle(sur, oracle, n):
+    p = init_params(seed=12)
+    sur.set_params(1, p)
+    x, t = data(n, seed=n)
+    loss, g = sur.gradient(1, x, t)
+    loss_o, g_o = oracle.mlp_grad(p, x, t)
+    assert abs(loss - loss_o) <= 1e-3 * loss_o
+    for k, (off, shape) in sg.OFFSETS.items():
+        m = int(np.prod(shape))
+        a, b = g[off:off + m].astype(np.float64), g_o[off:off + m]
+        rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+        assert rel < 1e-2, (k, rel)
+
+
+def test_training_fits_a_smooth_function(engine):
+    s = sg.Surrogate(engine, members=1, batch_rows=4096, seed=5, lr=3e-3, lr_final=1e-4)
+    x, t = data(60000, seed=21)
+    s.add_rows(x, t)
+    loss = s.train(30)
+    xt, tt = data(5000, seed=22)
+    err = s.forward(0, xt) - tt
+    assert loss[0] < 2e-3 and np.sqrt(np.mean(err ** 2)) < 0.05, (loss, np.sqrt(np.mean(err ** 2)))
+    s.close()
+
+
+def random_sims(n, seed, particles):
+    rng = np.random.default_rng(seed)
+    sims = []
+    for _ in range(n):
+        sims.append(make_sim(abi.GELIO_MODEL_2D_GELIOSPHERE, particles, K0_cm2s=float(rng.uniform(1e22, 1e23)),
+                             V_kms=float(rng.uniform(350, 750)), tilt_deg=float(rng.uniform(5, 75)),
+                             polarity=int(rng.choice([-1, 1])), r_injection=float(rng.uniform(1, 80)),
+                             theta_deg=float(rng.uniform(10, 170)), injection=abi.GELIO_INJ_LOG_GRID,
+                             inj_min=0.01, inj_max=100.0, inj_points=100, seed=int(rng.integers(1, 2**40))))
+    return sims
+
+
+def test_mc_trained_surrogate_and_fallback(engine):
+    """Trained on 192 Monte Carlo spectra (2e5 particles each) over the
+    batch parameter ranges, the ensemble reproduces held-out 1e6-particle
+    spectra over 0.1-10 GeV to a few percent; a simulation outside the
+    trained ranges shows a large ensemble spread and is answered by the
+    Monte Carlo."""
+    train = random_sims(192, 1, 200_000)
+    res = engine.run(train)
+    s = sg.Surrogate(engine, members=3, batch_rows=4096, seed=9, min_count=32)
+    rows = s.add_spectra(train, res.spectra)
+    assert rows > 100 * 150
+    s.train(60)
+    test = random_sims(8, 2, 1_000_000)
+    mc = engine.run(test)
+    pred, sd = s.predict(test)
+    errs = []
+    for i, sim in enumerate(test):
+        T = sg.grid_energies(sim)
+        ref = sg.mc_ln_ratio(mc.spectra[i], sim, lis=1, min_count=200)
+        sel = (T >= 0.1) & (T <= 10) & np.isfinite(ref)
+        errs.append(np.abs(np.exp(pred[i][sel] - ref[sel]) - 1.0))
+    med = float(np.median(np.concatenate(errs)))
+    assert med < 0.06, med
+    # outside the trained ranges (K0, V, tilt): spread, the Monte Carlo answers
+    odd = make_sim(abi.GELIO_MODEL_2D_GELIOSPHERE, 100_000, r_injection=1.0, K0_cm2s=1e21, V_kms=1400.0,
+                   tilt_deg=89.0, polarity=1, injection=abi.GELIO_INJ_LOG_GRID, inj_min=0.01, inj_max=100.0,
+                   inj_points=100, seed=4)
+    r, sdev, used = s.spectra([test[0], odd])
+    assert used[1] and np.all(sdev[1] == 0.0)
+    s.close()

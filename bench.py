@@ -69,6 +69,25 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(x: float, device: str = "cpu") -> float:
+    """The largest x over all ranks (x itself when not distributed): the
+    timed region of the job is that of its slowest rank."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def weak_scaling_value(units_per_rank: int, steps: int, t_ms_max: float, world: int) -> float:
+    """Whole-job throughput: every rank processed units_per_rank per step
+    (independent replicas with their own seeds, no data-path collective)."""
+    return world * units_per_rank * steps / (t_ms_max / 1e3)
+
+
 def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -380,8 +399,10 @@ def run_surrogate(args, eng, rank, world, local):
             "fallback_fraction": fb / len(test),
             "train_loss": [float(v) for v in loss], "seconds": {"mc_training_data": t_data, "training": t_train,
                                                                  "mc_test": mc_s, "surrogate_predict": t_pred},
-            "e2e": {"value": sur_rate, "unit": "spectra/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "gpu_launches": None}
+            "e2e": {"value": sur_rate, "unit": "spectra/s",
+                    "h2d_bytes_per_step": len(test) * 100 * 7 * 4,
+                    "d2h_bytes_per_step": len(test) * 100 * 5 * 4},
+            "gpu_launches": -(-len(test) * 100 // 16384) * (1 + 5 * 4)}
     print(json.dumps(line), flush=True)
     sur.close()
 
@@ -471,19 +492,13 @@ def main():
             step_ms.append(e0.elapsed_time(e1))
             kernel_ms.append(eng.last_stats().kernel_ms)
     torch.cuda.synchronize()
-    t_rank = sum(step_ms)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([t_rank], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dist.barrier()
-        t_rank = float(t.item())
+    t_rank = max_over_ranks(sum(step_ms), f"cuda:{local}")
     out = (abi.Spectra * n).from_buffer_copy(d_out.cpu().numpy().tobytes())
     specs = [spectra_dict(out[i]) for i in range(n)]
     steps_per_run = sum(s["n_steps"] for s in specs)
     assert all(int(s["n_particles"]) == sims[i].n_particles for i, s in enumerate(specs)), "incomplete run"
 
-    value = world * total_traj * args.steps / (t_rank / 1e3)
+    value = weak_scaling_value(total_traj, args.steps, t_rank, world)
 
     # e2e through the host-buffer C-ABI call
     host_out = (abi.Spectra * n)()
@@ -522,7 +537,7 @@ def main():
                 "e2e": {"value": e2e_value, "unit": "trajectories/s",
                         "h2d_bytes_per_step": n * ctypes.sizeof(abi.SimParams),
                         "d2h_bytes_per_step": n * ctypes.sizeof(abi.Spectra)},
-                "gpu_launches": 3 * args.steps, "fp64_steps": fp64, "clocks": clk.summary()}
+                "gpu_launches": 6 * args.steps, "fp64_steps": fp64, "clocks": clk.summary()}
         print(json.dumps(line), flush=True)
         eng.close()
         return
@@ -536,8 +551,8 @@ def main():
     tfile = os.path.join(ROOT, "profiles", "k_persistent_geliosphere_fp32_dram.txt")
     if os.path.exists(tfile):
         for ln in open(tfile):
-            if ln.startswith("dram_bytes_per_particle_step:"):
-                traffic = float(ln.split(":")[1]) * steps_per_run
+            if ln.startswith("dram_bytes_per_launch:"):
+                traffic = float(ln.split(":")[1])
     line = {
         "metric": "2D Geliosphere trajectories/s",
         "value": value,
@@ -557,21 +572,24 @@ def main():
         "e2e": {"value": e2e_value, "unit": "trajectories/s",
                 "h2d_bytes_per_step": n * ctypes.sizeof(abi.SimParams),
                 "d2h_bytes_per_step": n * ctypes.sizeof(abi.Spectra)},
-        "gpu_launches": 3 * args.steps,
+        "gpu_launches": 6 * args.steps,
+        # The reference step's algorithmic work binds on the special-function
+        # unit: 117 XU ops at the XU rate take longer than 316 FP32 ops at the
+        # FMA rate, so the XU roofline is the headline, FP32 beside it.
         "roofline": {
-            "bound": "fp32",
-            "achieved": achieved_tflops,
-            "peak": fp32_tflops,
-            "unit": "TFLOP/s",
-            "frac": achieved_tflops / fp32_tflops,
+            "bound": "sfu",
+            "achieved": achieved_xu,
+            "peak": xu_gops,
+            "unit": "Gop/s",
+            "frac": achieved_xu / xu_gops,
             "traffic": traffic,
             "kernel": "k_persistent<2D Geliosphere, float>",
             "kernel_ms": k_ms,
-            "alg_flop_per_particle_step": ALG_FLOP_PER_STEP,
-            "peak_source": "measured in this run by gelio_measure_peaks (FP32 FMA chains); "
-                           "MEASURED_PEAKS.json holds no FP32 SIMT figure",
-            "xu": {"achieved_gops": achieved_xu, "peak_gops": xu_gops, "frac": achieved_xu / xu_gops,
-                   "alg_xu_per_particle_step": ALG_XU_PER_STEP},
+            "alg_xu_per_particle_step": ALG_XU_PER_STEP,
+            "peak_source": "measured in this run by gelio_measure_peaks (ex2.approx chains, special-function "
+                           "unit; FP32 FMA chains); MEASURED_PEAKS.json holds no SFU or FP32 SIMT figure",
+            "fp32": {"achieved_tflops": achieved_tflops, "peak_tflops": fp32_tflops,
+                     "frac": achieved_tflops / fp32_tflops, "alg_flop_per_particle_step": ALG_FLOP_PER_STEP},
         },
         "clocks": clk.summary(),
     }

@@ -125,6 +125,8 @@ struct gelio_surrogate {
   std::vector<float> feats, targ;
   float *d_feats = nullptr, *d_targ = nullptr;
   size_t d_rows_cap = 0, d_rows_used = 0;
+  float *d_query = nullptr, *d_yq = nullptr;   // inference inputs / outputs
+  size_t query_cap = 0;
   bool dirty = true;
   std::mutex mu;
 };
@@ -184,7 +186,7 @@ void free_all(gelio_surrogate *s) {
   for (int i = 0; i < 4; ++i) { f(s->Z[i]); f(s->XT[i]); f(s->dH[i]); f(s->dHT[i]); }
   for (int i = 0; i < 3; ++i) f(s->X[i]);
   f(s->yhat); f(s->y); f(s->dy); f(s->partial); f(s->grad); f(s->loss_part); f(s->step_loss);
-  f(s->ident); f(s->order); f(s->error); f(s->d_feats); f(s->d_targ);
+  f(s->ident); f(s->order); f(s->error); f(s->d_feats); f(s->d_targ); f(s->d_query); f(s->d_yq);
   if (s->stream) cudaStreamDestroy(s->stream);
 }
 
@@ -280,6 +282,34 @@ int stage_rows(gelio_surrogate *s, float *d_x, float *d_t, int n) {
 }
 
 bool valid_member(gelio_surrogate *s, int m) { return s && m >= 0 && m < (int)s->mem.size(); }
+
+// Inference of members [m0, m1) on n rows x [n][7]: one upload, one gather
+// per batch of rows shared by the members, outputs y[(m - m0) * n + row].
+int infer_rows(gelio_surrogate *s, int m0, int m1, const float *x, size_t n, float *y) {
+  if (n == 0) return GELIO_OK;
+  const size_t E = (size_t)(m1 - m0);
+  if (n > s->query_cap) {
+    if (s->d_query) cudaFree(s->d_query);
+    if (s->d_yq) cudaFree(s->d_yq);
+    s->d_query = s->d_yq = nullptr;
+    s->query_cap = 0;
+    SUR_TRY(cudaMalloc(&s->d_query, n * kFeatures * 4));
+    SUR_TRY(cudaMalloc(&s->d_yq, n * 16 * 4));
+    s->query_cap = n;
+  }
+  SUR_TRY(cudaMemcpyAsync(s->d_query, x, n * kFeatures * 4, cudaMemcpyHostToDevice, s->stream));
+  for (size_t off = 0; off < n; off += (size_t)s->rows) {
+    const int c = (int)std::min<size_t>((size_t)s->rows, n - off);
+    int rc = stage_rows(s, s->d_query + off * kFeatures, nullptr, c);
+    if (rc != GELIO_OK) return rc;
+    for (size_t e = 0; e < E; ++e) {
+      if ((rc = forward_infer(s, s->mem[m0 + e])) != GELIO_OK) return rc;
+      SUR_TRY(cudaMemcpyAsync(s->d_yq + e * n + off, s->yhat, (size_t)c * 4, cudaMemcpyDeviceToDevice, s->stream));
+    }
+  }
+  SUR_TRY(cudaMemcpyAsync(y, s->d_yq, E * n * 4, cudaMemcpyDeviceToHost, s->stream));
+  return check_error(s);
+}
 
 void default_opts(gelio_surrogate_opts &o) {
   std::memset(&o, 0, sizeof(o));
@@ -556,22 +586,7 @@ int32_t gelio_surrogate_forward(gelio_surrogate *s, int32_t member, const float 
   if (!valid_member(s, member) || n < 0 || (n > 0 && (!x || !y))) return GELIO_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lock(s->mu);
   SUR_TRY(cudaSetDevice(s->device));
-  float *d_x = nullptr;
-  SUR_TRY(cudaMalloc(&d_x, (size_t)std::max(n, 1) * kFeatures * 4));
-  int rc = GELIO_OK;
-  for (int off = 0; off < n && rc == GELIO_OK; off += s->rows) {
-    const int c = std::min(s->rows, n - off);
-    if (cudaMemcpyAsync(d_x, x + (size_t)off * kFeatures, (size_t)c * kFeatures * 4, cudaMemcpyHostToDevice,
-                        s->stream) != cudaSuccess) { rc = GELIO_ERR_CUDA; break; }
-    if ((rc = stage_rows(s, d_x, nullptr, c)) != GELIO_OK) break;
-    if ((rc = forward_infer(s, s->mem[member])) != GELIO_OK) break;
-    if (cudaMemcpyAsync(y + off, s->yhat, (size_t)c * 4, cudaMemcpyDeviceToHost, s->stream) != cudaSuccess)
-      rc = GELIO_ERR_CUDA;
-    if (rc == GELIO_OK) rc = check_error(s);
-  }
-  cudaStreamSynchronize(s->stream);
-  cudaFree(d_x);
-  return rc;
+  return infer_rows(s, member, member + 1, x, (size_t)n, y);
 }
 
 int32_t gelio_surrogate_gradient(gelio_surrogate *s, int32_t member, const float *x, const float *t, int32_t n,
@@ -650,8 +665,10 @@ int32_t gelio_surrogate_predict(gelio_surrogate *s, const gelio_sim_params *sims
   if (rows == 0) return GELIO_OK;
   const int E = (int)s->mem.size();
   std::vector<float> y((size_t)E * rows);
-  for (int e = 0; e < E; ++e) {
-    int rc = gelio_surrogate_forward(s, e, x.data(), (int32_t)rows, y.data() + (size_t)e * rows);
+  {
+    std::lock_guard<std::mutex> lock(s->mu);
+    SUR_TRY(cudaSetDevice(s->device));
+    const int rc = infer_rows(s, 0, E, x.data(), rows, y.data());
     if (rc != GELIO_OK) return rc;
   }
   for (size_t r = 0; r < rows; ++r) {

@@ -358,14 +358,16 @@ def run_surrogate(args, eng, rank, world, local):
         res = eng.run(part)
         mc_s += time.perf_counter() - t2
         ref += [sg.mc_ln_ratio(res.spectra[i], part[i], lis=1, min_count=100) for i in range(len(part))]
-    # the same draws at the training statistics: what the MC alone gives at that cost
-    small = [sim for sim in test[:min(len(test), 200)]]
+    # the same draws at the training statistics with independent random
+    # streams: the error of the Monte Carlo alone at the cost of one
+    # training spectrum
+    from geliosphere_gb300 import abi
+    small = [abi.SimParams.from_buffer_copy(sim) for sim in test[:min(len(test), 200)]]
     for sim in small:
         sim.n_particles = args.surr_train_particles
+        sim.seed = (sim.seed * 0x9E3779B97F4A7C15 + 0x632BE59BD9B4E019) & 0xFFFFFFFFFFFFFFFF
     res_small = eng.run(small)
     low = [sg.mc_ln_ratio(res_small.spectra[i], small[i], lis=1, min_count=1) for i in range(len(small))]
-    for sim in small:
-        sim.n_particles = args.surr_test_particles
     # surrogate: warm-up, then timed
     sur.predict(test[:chunk])
     t3 = time.perf_counter()
@@ -396,6 +398,7 @@ def run_surrogate(args, eng, rank, world, local):
             "mc_spectra_per_s": mc_rate, "surrogate_over_mc": sur_rate / mc_rate,
             "median_abs_dflux_0p1_10GeV": med,
             "mc_at_training_statistics_median_abs_dflux": med_mc,
+            "mc_particles_for_surrogate_error": args.surr_train_particles * (med_mc / med) ** 2,
             "fallback_fraction": fb / len(test),
             "train_loss": [float(v) for v in loss], "seconds": {"mc_training_data": t_data, "training": t_train,
                                                                  "mc_test": mc_s, "surrogate_predict": t_pred},

@@ -65,9 +65,15 @@ def cpu_pins():
         "geliosphere": (base_args(500), [(0, 8, 0, 12345), (3, 8, 1, 777)]),
         "solarprop": (base_args(500, uniform=1), [(0, 8, 0, 4242), (5, 8, 2, 99)]),
         "bp": (base_args(200), [(0, 8, 0, 2024), (7, 8, 3, 31337)]),
-        "fp": (base_args(50), [(0, 8, 0, 5), (2, 8, 1, 6), (1, 4, 0, 7)]),
+        # 1 AU crossings are rare (~1e-4 per particle): 120 blocks give a few
+        # hundred crossing records
+        "fp": (base_args(50), [(0, 8, 0, 5), (2, 8, 1, 6), (1, 4, 0, 7)] +
+               [(k % 8, 8, k // 8, 100 + k) for k in range(120)]),
     }
+    only = [a.split("=", 1)[1] for a in sys.argv if a.startswith("--pins=")]
     for model, (args, blocks) in cases.items():
+        if only and model not in only[0].split(","):
+            continue
         resolved, per_block = run_ref(model, args, blocks)
         doc = {"model": model, "args": args, "resolved": resolved, "blocks": []}
         for spec, rows in zip(blocks, per_block):
@@ -198,6 +204,8 @@ def main():
     ffi.build()
     rng = np.random.default_rng(20240601)
     cpu_pins()
+    if any(a.startswith("--pins=") for a in sys.argv):
+        return
     eval_goldens(rng)
     if "--skip-spectra" not in sys.argv:
         spectra_goldens()

@@ -79,6 +79,7 @@ struct BatchRow {          // struct batchRunInput (Algorithm/include/BatchRun.h
   std::string model, pathToCustomSettingsFile, name;
 };
 
+// BatchRun::getValuesForSingleSimulation (Algorithm/src/BatchRun.cpp:102-193)
 void readRow(const CsvTable &t, size_t i, BatchRow &b) {
   auto warn = [](const char *c) { glog::warn(std::string("Column ") + c + " is not defined."); };
   if (t.has("name")) b.name = t.str("name", i); else warn("name");
@@ -95,7 +96,7 @@ void readRow(const CsvTable &t, size_t i, BatchRow &b) {
   else warn("pathToCustomSettingsFile");
 }
 
-// BatchRun::validateInputForSimulation (BatchRun.cpp:238-265)
+// BatchRun::validateInputForSimulation (Algorithm/src/BatchRun.cpp:254-280)
 bool validateRow(const BatchRow &b) {
   const bool twoD = (b.model == "2D Geliosphere" || b.model == "2D SolarProp-like");
   if (!twoD && b.theta != -1.0) glog::warn("Setting of theta for 1D models does not have any effect on simulation");
@@ -114,7 +115,7 @@ bool validateRow(const BatchRow &b) {
   return true;
 }
 
-// BatchRun::parseValues (BatchRun.cpp:267-329); the row's settings are
+// BatchRun::parseValues (Algorithm/src/BatchRun.cpp:282-342); the row's settings are
 // merged in memory instead of through a file under /tmp.
 bool parseRow(ParamsCarrier *p, const BatchRow &b) {
   if (b.dt != -1.0) {
@@ -132,9 +133,13 @@ bool parseRow(ParamsCarrier *p, const BatchRow &b) {
   }
   if (b.V != -1.0) {
     // the reference returns -1 from a bool function here, i.e. true: the row
-    // still runs with V unset (BatchRun.cpp:298-302); kept.
-    if (!validation::checkV((float)b.V)) glog::error("V is out of range!(100-1500 km/s)");
-    else validation::setV(p, (float)b.V);
+    // runs at once, with V unset and without its name, settings or dates
+    // (Algorithm/src/BatchRun.cpp:316-321); kept.
+    if (!validation::checkV((float)b.V)) {
+      glog::error("V is out of range!(100-1500 km/s)");
+      return true;
+    }
+    validation::setV(p, (float)b.V);
   }
   if (!b.name.empty()) {
     if (b.name.find_first_not_of(' ') != std::string::npos) p->putString("destination", b.name);
@@ -151,7 +156,7 @@ bool parseRow(ParamsCarrier *p, const BatchRow &b) {
   return true;
 }
 
-// BatchRun::validateInputBatchFile (BatchRun.cpp:331-352)
+// BatchRun::validateInputBatchFile (Algorithm/src/BatchRun.cpp:344-365)
 bool uniqueNames(const CsvTable &t) {
   std::vector<std::string> names;
   for (size_t i = 0; i < t.rows.size(); ++i) {
@@ -214,8 +219,9 @@ void BatchRun::runAlgorithm(ParamsCarrier *p) {
     p->putString("model", b.model);
     const int model = ghost::modelFromName(b.model);
     if (model < 0) {
+      // as in the reference, a skipped row leaves its values in the map
+      // (Algorithm/src/BatchRun.cpp:64-70 continues without eraseAllItems)
       glog::error("Selected model for simulation " + std::to_string(row) + " is not supported in batch mode.");
-      p->eraseAllItems(excluded);
       continue;
     }
     std::string dest = p->getString("destination", "");

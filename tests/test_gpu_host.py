@@ -4,6 +4,7 @@ the written log.dat (--evaluation); batch mode as one launch equal to the
 same rows run one by one (same particles, same counts; bin sums equal to
 FP64 accumulation-order noise)."""
 import os
+import pathlib
 import subprocess
 
 import numpy as np
@@ -145,3 +146,16 @@ def test_batch_one_launch_equals_single_runs(exe, tmp_path):
         ref = single / "results" / d / "s"
         for f in files:
             same_table(got / f, ref / f, f)
+
+
+@pytest.mark.parametrize("flag,d,files", [("-T", "eval_2d", SPECTRA_2D), ("-B", "eval_bp", SPECTRA_1D),
+                                          ("-F", "eval_fp", SPECTRA_1D)])
+def test_cli_evaluation_reproduces_reference_evaluator_files(exe, tmp_path, flag, d, files):
+    """--evaluation on the committed log.dat fixtures: the GPU evaluation
+    writes the spectrum files the reference evaluators wrote (tests/golden)."""
+    from conftest import GOLDEN
+    src = os.path.join(GOLDEN, d)
+    rc, err = run(exe, [flag, "--evaluation", os.path.join(src, "log.dat")], tmp_path)
+    assert rc == 0, err
+    for f in files:
+        same_table(tmp_path / f, pathlib.Path(src) / f, f)

@@ -1,6 +1,8 @@
 """The surrogate network's GPU kernels (tcgen05 GEMMs with fused epilogues)
 against the CPU restatement: forward outputs and every parameter gradient;
 then training on the GPU and the fallback to the Monte Carlo."""
+import time
+
 import numpy as np
 import pytest
 
@@ -82,19 +84,54 @@ def test_mc_trained_surrogate_and_fallback(engine):
     s.train(60)
     test = random_sims(8, 2, 1_000_000)
     mc = engine.run(test)
+    t_mc = mc.stats.total_ms
+    t0 = time.perf_counter()
     pred, sd = s.predict(test)
-    errs = []
+    t_sur = 1e3 * (time.perf_counter() - t0)
+    # what the network gains: the same draws by the Monte Carlo alone at the
+    # cost of one training spectrum (2e5 particles, independent streams)
+    low = random_sims(8, 2, 200_000)
+    for sim in low:
+        sim.seed ^= 0x5DEECE66D
+    mc_low = engine.run(low)
+    errs, errs_low = [], []
     for i, sim in enumerate(test):
         T = sg.grid_energies(sim)
         ref = sg.mc_ln_ratio(mc.spectra[i], sim, lis=1, min_count=200)
         sel = (T >= 0.1) & (T <= 10) & np.isfinite(ref)
         errs.append(np.abs(np.exp(pred[i][sel] - ref[sel]) - 1.0))
+        lo = sg.mc_ln_ratio(mc_low.spectra[i], low[i], lis=1, min_count=1)
+        sel2 = sel & np.isfinite(lo)
+        errs_low.append(np.abs(np.exp(lo[sel2] - ref[sel2]) - 1.0))
     med = float(np.median(np.concatenate(errs)))
+    med_low = float(np.median(np.concatenate(errs_low)))
+    print(f"surrogate median |dflux| {med:.4f} in {t_sur:.2f} ms; MC at 2e5 particles {med_low:.4f}; "
+          f"MC at 1e6 particles {t_mc:.1f} ms")
     assert med < 0.06, med
+    assert med < 2.0 * med_low + 0.01, (med, med_low)
+    assert t_sur * 20 < t_mc, (t_sur, t_mc)
     # outside the trained ranges (K0, V, tilt): spread, the Monte Carlo answers
     odd = make_sim(abi.GELIO_MODEL_2D_GELIOSPHERE, 100_000, r_injection=1.0, K0_cm2s=1e21, V_kms=1400.0,
                    tilt_deg=89.0, polarity=1, injection=abi.GELIO_INJ_LOG_GRID, inj_min=0.01, inj_max=100.0,
                    inj_points=100, seed=4)
     r, sdev, used = s.spectra([test[0], odd])
     assert used[1] and np.all(sdev[1] == 0.0)
+    s.close()
+
+
+def test_training_is_deterministic_and_params_round_trip(engine):
+    """Same seed, same rows -> bit-identical parameters (fixed-order split-K
+    reductions, no atomics in the gradient); get/set round trip."""
+    x, t = data(9000, seed=31)
+    ps = []
+    for _ in range(2):
+        s = sg.Surrogate(engine, members=1, batch_rows=4096, seed=17)
+        s.add_rows(x, t)
+        s.train(3)
+        ps.append(s.get_params(0))
+        s.close()
+    np.testing.assert_array_equal(ps[0], ps[1])
+    s = sg.Surrogate(engine, members=2, batch_rows=4096, seed=18)
+    s.set_params(1, ps[0])
+    np.testing.assert_array_equal(s.get_params(1), ps[0])
     s.close()

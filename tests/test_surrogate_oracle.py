@@ -89,3 +89,16 @@ def test_oracle_matches_numpy_to_bf16_precision(oracle):
         a, b = g_or[off:off + n], g_np[off:off + n]
         rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
         assert rel < 3e-2, (k, rel)
+
+
+def test_feature_normalisation():
+    """gelio_surrogate_features (host function, no GPU) maps the batch
+    parameter ranges onto [-1, 1]."""
+    from geliosphere_gb300 import abi, make_sim
+    from geliosphere_gb300.surrogate import Surrogate
+    lo = make_sim(abi.GELIO_MODEL_2D_GELIOSPHERE, 1, K0_cm2s=1e22, V_kms=350, tilt_deg=5, polarity=-1,
+                  r_injection=1.0, theta_deg=10)
+    hi = make_sim(abi.GELIO_MODEL_2D_GELIOSPHERE, 1, K0_cm2s=1e23, V_kms=750, tilt_deg=75, polarity=1,
+                  r_injection=80.0, theta_deg=170)
+    np.testing.assert_allclose(Surrogate.features(lo, 0.01), [-1] * 7, atol=2e-6)
+    np.testing.assert_allclose(Surrogate.features(hi, 100.0), [1] * 7, atol=2e-6)

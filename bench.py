@@ -61,7 +61,9 @@ def parse():
     ap.add_argument("--surr-test", type=int, default=2000, help="surrogate: held-out parameter draws")
     ap.add_argument("--surr-test-particles", type=int, default=10_000_000)
     ap.add_argument("--surr-epochs", type=int, default=40)
-    ap.add_argument("--workload", default="geliosphere", choices=["geliosphere", "bp", "fp", "batch256", "surrogate"],
+    ap.add_argument("--batch-scale", type=float, default=1.0, help="batch256: particle-count scale (profiling)")
+    ap.add_argument("--workload", default="geliosphere",
+                    choices=["geliosphere", "bp", "fp", "batch256", "batch_cli", "surrogate"],
                     help="geliosphere: the headline 4-case 2D run (default); bp: 1D B-p 1e7 on a 100-point "
                          "log grid, FP32 and FP64 steps; fp: 1D F-p 1e6 log-uniform, 300 log bins; batch256: "
                          "256 random 2D simulations in one launch vs 256 plain launches; surrogate: train the "
@@ -267,7 +269,7 @@ def run_batch256(args, eng, rank, world, local):
     import ctypes
     import torch
     from geliosphere_gb300 import abi
-    sims = workload_batch256(rank)
+    sims = workload_batch256(rank, scale=args.batch_scale)
     n = len(sims)
     total = sum(s.n_particles for s in sims)
     tune = None if args.no_tune else eng.autotune(workload_batch256(rank, scale=0.05))
@@ -310,6 +312,63 @@ def run_batch256(args, eng, rank, world, local):
             "persistent_over_plain": persistent / plain,
             "particle_steps_per_s": r.stats.n_steps / (sum(times) / args.steps),
             "gpu_launches": 3 * args.steps, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
+def run_batch_cli(args, rank, world):
+    """The batch workload through the reference-facing command line: a
+    256-row batch CSV (K0, V, r, theta per row, tilt per row through a
+    per-row settings file, N = 1 million each: the CSV counts particles in
+    whole millions and polarity has no CSV or settings key) run by the
+    `geliosphere -b` executable, which resolves the rows like the reference
+    and runs them in one persistent launch; wall time including parsing,
+    directories and all spectrum files."""
+    import tempfile
+    import numpy as np
+    from geliosphere_gb300 import host
+    host.build()
+    rng = np.random.default_rng(20240)
+    work = tempfile.mkdtemp(prefix="gelio_batch_")
+    rows = []
+    for i in range(256):
+        st = os.path.join(work, f"s{i}.toml")
+        with open(st, "w") as f:
+            f.write("[default_values]\nK0 = 5e22\nV = 400.0\ndt = 500.0\nr_injection = 1.0\n"
+                    "uniform_energy_injection_maximum = 101.0\n[2d_models_common_settings]\n"
+                    "theta_injection = 90.0\nuse_uniform_injection = false\n[SolarProp_like_model_settings]\n"
+                    "SolarProp_ratio = 0.02\n[Geliosphere_model_settings]\nGeliosphere_ratio = 0.2\n"
+                    "K0_ratio = 1.0\nC_delta = 8.7e-5\ndefault_tilt_angle = %.3f\n[advanced_settings]\n"
+                    "remove_log_files_after_simulation = true\n" % rng.uniform(5, 75))
+        rows.append("r%d,,,%.1f,%.4e,,%.3f,%.3f,1,2D Geliosphere,%s" % (
+            i, rng.uniform(350, 750), rng.uniform(1e22, 1e23), rng.uniform(1, 80), rng.uniform(10, 170), st))
+    csv = os.path.join(work, "batch.csv")
+    with open(csv, "w") as f:
+        f.write("name,month,year,V,K0,dt,r,theta,N,model,pathToCustomSettingsFile\n" + "\n".join(rows) + "\n")
+    times = []
+    for k in range(args.warmup + args.steps):
+        d = os.path.join(work, f"run{k}")
+        os.makedirs(d)
+        t0 = time.perf_counter()
+        r = subprocess.run([host.EXE, "-b", csv], cwd=d, capture_output=True, text=True)
+        dt = time.perf_counter() - t0
+        if r.returncode != 0:
+            raise RuntimeError(r.stderr[-2000:])
+        if k >= args.warmup:
+            times.append(dt)
+    n = sum(1 for _ in os.scandir(os.path.join(work, f"run{args.warmup}", "results", "Geliosphere2D")))
+    assert n == 256, n
+    particles = 256 * (-(-1_000_000 // 4096) * 4096)
+    if rank != 0:
+        return
+    v = particles * len(times) / sum(times)
+    line = {"metric": "batched 2D Geliosphere trajectories/s (command line)", "value": v,
+            "unit": "trajectories/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": run_batch_cli.__doc__.replace("\n", " "), "rows": 256, "particles": particles},
+            "e2e": {"value": v, "unit": "trajectories/s", "h2d_bytes_per_step": 256 * 96,
+                    "d2h_bytes_per_step": 256 * 64808},
+            "gpu_launches": 3 * args.steps}
     print(json.dumps(line), flush=True)
 
 
@@ -373,6 +432,13 @@ def run_surrogate(args, eng, rank, world, local):
     t3 = time.perf_counter()
     pred, sd = sur.predict(test)
     t_pred = time.perf_counter() - t3
+    dev_ms, flop = sur.last_inference()
+    peaks = {}
+    pfile = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pfile):
+        peaks = json.load(open(pfile))
+    bf16_peak = peaks.get("bf16_tflops", 1900.0)
+    achieved = flop / (dev_ms / 1e3) / 1e12 if dev_ms > 0 else 0.0
     errs, errs_mc, fb = [], [], 0
     for i, sim in enumerate(test):
         T = sg.grid_energies(sim)
@@ -405,7 +471,12 @@ def run_surrogate(args, eng, rank, world, local):
             "e2e": {"value": sur_rate, "unit": "spectra/s",
                     "h2d_bytes_per_step": len(test) * 100 * 7 * 4,
                     "d2h_bytes_per_step": len(test) * 100 * 5 * 4},
-            "gpu_launches": -(-len(test) * 100 // 16384) * (1 + 5 * 4)}
+            "gpu_launches": -(-len(test) * 100 // 16384) * (1 + 5 * 4),
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
+                         "frac": achieved / bf16_peak, "traffic": None, "kernel": "k_mlp_gemm<INFER*> (tcgen05)",
+                         "device_ms": dev_ms, "flop": flop,
+                         "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if peaks else
+                                        "fallback 1.9 PFLOP/s bf16 burst"}}
     print(json.dumps(line), flush=True)
     sur.close()
 
@@ -429,6 +500,9 @@ def main():
     from geliosphere_gb300 import abi, Engine
     from geliosphere_gb300.engine import spectra_dict
 
+    if args.workload == "batch_cli":
+        run_batch_cli(args, rank, world)
+        return
     torch.cuda.set_device(local)
     eng = Engine(local)
     if args.workload in ("batch256", "surrogate"):
@@ -586,6 +660,7 @@ def main():
             "unit": "Gop/s",
             "frac": achieved_xu / xu_gops,
             "traffic": traffic,
+            "output_path_gbs": (traffic / (k_ms / 1e3) / 1e9) if traffic else None,
             "kernel": "k_persistent<2D Geliosphere, float>",
             "kernel_ms": k_ms,
             "alg_xu_per_particle_step": ALG_XU_PER_STEP,

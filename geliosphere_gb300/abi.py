@@ -164,6 +164,7 @@ PROTOTYPES = {
                                           POINTER(c_double)]),
     "gelio_surrogate_spectra": (c_int32, [c_void_p, POINTER(SimParams), c_int32, POINTER(RunOpts),
                                           POINTER(c_double), POINTER(c_double), POINTER(c_int32)]),
+    "gelio_surrogate_last_inference": (c_int32, [c_void_p, POINTER(c_double), POINTER(c_double)]),
     "gelio_surrogate_get_params": (c_int32, [c_void_p, c_int32, POINTER(c_float)]),
     "gelio_surrogate_set_params": (c_int32, [c_void_p, c_int32, POINTER(c_float)]),
     "gelio_surrogate_forward": (c_int32, [c_void_p, c_int32, POINTER(c_float), c_int32, POINTER(c_float)]),

@@ -127,6 +127,8 @@ struct gelio_surrogate {
   size_t d_rows_cap = 0, d_rows_used = 0;
   float *d_query = nullptr, *d_yq = nullptr;   // inference inputs / outputs
   size_t query_cap = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;    // device time of the last inference
+  double last_ms = 0.0, last_flop = 0.0;
   bool dirty = true;
   std::mutex mu;
 };
@@ -152,7 +154,7 @@ int launch_gemm(gelio_surrogate *s, const CUtensorMap &A, const CUtensorMap &B, 
   if (a.k_per_split <= 0) a.k_per_split = a.K;
   const int tiles = ((a.M + kTileM - 1) / kTileM) * a.splits;
   const int grid = std::max(1, std::min(tiles, s->sm_count));
-  k_mlp_gemm<MODE><<<grid, kThreads, kGemmSmem, s->stream>>>(A, B, a);
+  k_mlp_gemm<MODE><<<grid, kGemmThreads, kGemmSmem, s->stream>>>(A, B, a);
   return cuda_status(cudaGetLastError());
 }
 
@@ -187,6 +189,8 @@ void free_all(gelio_surrogate *s) {
   for (int i = 0; i < 3; ++i) f(s->X[i]);
   f(s->yhat); f(s->y); f(s->dy); f(s->partial); f(s->grad); f(s->loss_part); f(s->step_loss);
   f(s->ident); f(s->order); f(s->error); f(s->d_feats); f(s->d_targ); f(s->d_query); f(s->d_yq);
+  if (s->ev0) cudaEventDestroy(s->ev0);
+  if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->stream) cudaStreamDestroy(s->stream);
 }
 
@@ -298,7 +302,10 @@ int infer_rows(gelio_surrogate *s, int m0, int m1, const float *x, size_t n, flo
     s->query_cap = n;
   }
   SUR_TRY(cudaMemcpyAsync(s->d_query, x, n * kFeatures * 4, cudaMemcpyHostToDevice, s->stream));
+  SUR_TRY(cudaEventRecord(s->ev0, s->stream));
+  size_t padded = 0;
   for (size_t off = 0; off < n; off += (size_t)s->rows) {
+    padded += (size_t)s->rows;
     const int c = (int)std::min<size_t>((size_t)s->rows, n - off);
     int rc = stage_rows(s, s->d_query + off * kFeatures, nullptr, c);
     if (rc != GELIO_OK) return rc;
@@ -307,8 +314,18 @@ int infer_rows(gelio_surrogate *s, int m0, int m1, const float *x, size_t n, flo
       SUR_TRY(cudaMemcpyAsync(s->d_yq + e * n + off, s->yhat, (size_t)c * 4, cudaMemcpyDeviceToDevice, s->stream));
     }
   }
+  SUR_TRY(cudaEventRecord(s->ev1, s->stream));
   SUR_TRY(cudaMemcpyAsync(y, s->d_yq, E * n * 4, cudaMemcpyDeviceToHost, s->stream));
-  return check_error(s);
+  const int rc = check_error(s);
+  float ms = 0.f;
+  if (rc == GELIO_OK && cudaEventElapsedTime(&ms, s->ev0, s->ev1) == cudaSuccess) {
+    s->last_ms = ms;
+    // FLOP of the GEMMs over the rows actually multiplied (batches padded to
+    // batch_rows; first layer K padded to 64)
+    s->last_flop = 2.0 * (double)padded * (double)E *
+                   ((double)kInPad * kWidth + 3.0 * kWidth * kWidth + (double)kWidth);
+  }
+  return rc;
 }
 
 void default_opts(gelio_surrogate_opts &o) {
@@ -377,6 +394,7 @@ int32_t gelio_surrogate_create(gelio_ctx *ctx, const gelio_surrogate_opts *opts,
   if ((rc = set_smem_attrs()) != GELIO_OK) return fail(rc);
   cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device);
   if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(GELIO_ERR_CUDA);
+  if (cudaEventCreate(&s->ev0) != cudaSuccess || cudaEventCreate(&s->ev1) != cudaSuccess) return fail(GELIO_ERR_CUDA);
   const size_t R = (size_t)s->rows;
   auto alloc = [&](void **p, size_t bytes) {
     if (rc != GELIO_OK) return;
@@ -618,6 +636,14 @@ int32_t gelio_surrogate_gradient(gelio_surrogate *s, int32_t member, const float
   cudaFree(d_t);
   cudaFree(d_loss);
   return rc;
+}
+
+int32_t gelio_surrogate_last_inference(gelio_surrogate *s, double *device_ms, double *flop) {
+  if (!s) return GELIO_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lock(s->mu);
+  if (device_ms) *device_ms = s->last_ms;
+  if (flop) *flop = s->last_flop;
+  return GELIO_OK;
 }
 
 int32_t gelio_surrogate_get_params(gelio_surrogate *s, int32_t member, float *params) {

@@ -131,23 +131,39 @@ __device__ __forceinline__ void gemm_epilogue(const GemmArgs &a, int row, uint32
   if ((MODE == FWD_LAST || MODE == INFER_LAST) && valid) a.y_out[row] = ysum + __ldg(a.b5);
 }
 
-// One CTA per SM (the 4-stage ring takes 192 KiB of shared memory), tiles of
-// 128 GEMM rows handed out round-robin.  Thread 0 issues the TMA loads (up
-// to kStages chunks ahead) and the MMAs; all four warps run the epilogue,
-// warp w reading TMEM lanes 32w..32w+31 (one GEMM row per thread).
+// One CTA per SM, warp-specialised, tiles of 128 GEMM rows handed out
+// round-robin:
+//   warp 0  (one lane)  TMA producer: the weight operand once (resident in
+//           shared memory for the whole launch), then the row tiles of A
+//           through a 4-stage ring; for weight gradients (DW) both operands
+//           stream through the ring;
+//   warp 1  (one lane)  MMA issuer: tcgen05.mma into one of two TMEM
+//           accumulators (2 x 256 columns), tcgen05.commit frees a ring
+//           stage and hands a finished accumulator to the epilogue;
+//   warps 2-5           epilogue: tcgen05.ld one row per thread (warp w reads
+//           TMEM lanes 32 (w % 4) .. +31), fused epilogue, then hand the
+//           accumulator back; it overlaps the MMAs of the next tile.
+// Shared memory: region 1 (128 KiB) holds the resident weights (or the B
+// stages of DW), region 2 (64 KiB) the A stages.
+constexpr int kGemmThreads = 192;
+constexpr uint32_t kRegion1 = 4 * kStageB;         // 128 KiB
+constexpr uint32_t kRegion2 = kStages * kStageA;   // 64 KiB
+
 template <int MODE>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kGemmThreads, 1)
     k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const GemmArgs a) {
+  constexpr bool kResidentB = (MODE != DW);
   extern __shared__ unsigned char smem_raw[];
-  __shared__ int s_abort;
   const uint32_t s0 = tc::smem_u32(smem_raw);
   unsigned char *base = smem_raw + ((1024u - (s0 & 1023u)) & 1023u);
-  unsigned char *stA = base;
-  unsigned char *stB = base + kStages * kStageA;
-  uint64_t *full = reinterpret_cast<uint64_t *>(stB + kStages * kStageB);
+  unsigned char *r1 = base;
+  unsigned char *r2 = base + kRegion1;
+  uint64_t *full = reinterpret_cast<uint64_t *>(r2 + kRegion2);
   uint64_t *empty = full + kStages;
-  uint64_t *accum = empty + kStages;
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(accum + 1);
+  uint64_t *bfull = empty + kStages;
+  uint64_t *accf = bfull + 1;
+  uint64_t *acce = accf + 2;
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(acce + 2);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t bytesB = (uint32_t)a.N * kChunk * 2;
@@ -158,14 +174,17 @@ __global__ void __launch_bounds__(kThreads, 1)
       tc::mbar_init(&full[s], 1);
       tc::mbar_init(&empty[s], 1);
     }
-    tc::mbar_init(accum, 1);
+    tc::mbar_init(bfull, 1);
+    for (int b = 0; b < 2; ++b) {
+      tc::mbar_init(&accf[b], 1);
+      tc::mbar_init(&acce[b], 4);
+    }
     tc::fence_mbar_init();
     tc::tma_prefetch(&tmA);
     tc::tma_prefetch(&tmB);
-    s_abort = 0;
   }
-  if (warp == 0) {
-    tc::tmem_alloc(tslot, kTmemCols);
+  if (warp == 1) {
+    tc::tmem_alloc(tslot, 2 * kTmemCols);
     tc::tmem_relinquish();
   }
   tc::tc_fence_before();
@@ -173,75 +192,114 @@ __global__ void __launch_bounds__(kThreads, 1)
   tc::tc_fence_after();
   const uint32_t tmem = *tslot;
   const unsigned long long deadline = tc::now_ns() + a.timeout_ns;
-
   const int m_tiles = (a.M + kTileM - 1) / kTileM;
   const int tiles = m_tiles * a.splits;
-  uint32_t load_it = 0, mma_it = 0, acc_phase = 0;
-  for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
-    const int tm = t % m_tiles;
-    const int split = t / m_tiles;
-    const int k0 = split * a.k_per_split;
-    const int klen = min(a.k_per_split, a.K - k0);
-    const int nk = (klen + kChunk - 1) / kChunk;
-    if (nk <= 0) continue;
-    if (tid == 0 && !s_abort) {
+
+  if (warp == 0) {
+    if (lane == 0) {
+      uint32_t it = 0;
       bool ok = true;
-      int issued = 0;
-      for (int kc = 0; kc < nk && ok; ++kc) {
-        while (issued < nk && load_it < mma_it + kStages) {
-          const uint32_t st = load_it % kStages;
-          if (load_it >= (uint32_t)kStages && !tc::mbar_wait(&empty[st], ((load_it / kStages) - 1) & 1, deadline)) {
+      if (kResidentB) {
+        const int nkb = a.K / kChunk;
+        tc::mbar_expect_tx(bfull, (uint32_t)nkb * bytesB);
+        for (int c = 0; c < nkb; ++c) tc::tma_load_2d(r1 + c * kStageB, &tmB, c * kChunk, 0, bfull);
+      }
+      for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
+        const int tm = t % m_tiles, split = t / m_tiles;
+        const int k0 = split * a.k_per_split;
+        const int nk = (min(a.k_per_split, a.K - k0) + kChunk - 1) / kChunk;
+        for (int kc = 0; kc < nk; ++kc) {
+          const uint32_t st = it % kStages;
+          if (it >= (uint32_t)kStages && !tc::mbar_wait(&empty[st], ((it / kStages) - 1) & 1, deadline)) {
             ok = false;
             break;
           }
-          tc::mbar_expect_tx(&full[st], kStageA + bytesB);
-          tc::tma_load_2d(stA + st * kStageA, &tmA, k0 + issued * kChunk, tm * kTileM, &full[st]);
-          tc::tma_load_2d(stB + st * kStageB, &tmB, k0 + issued * kChunk, 0, &full[st]);
-          ++load_it;
-          ++issued;
+          tc::mbar_expect_tx(&full[st], kStageA + (kResidentB ? 0u : bytesB));
+          tc::tma_load_2d(r2 + st * kStageA, &tmA, k0 + kc * kChunk, tm * kTileM, &full[st]);
+          if (!kResidentB) tc::tma_load_2d(r1 + st * kStageB, &tmB, k0 + kc * kChunk, 0, &full[st]);
+          ++it;
         }
-        if (!ok) break;
-        const uint32_t st = mma_it % kStages;
-        if (!tc::mbar_wait(&full[st], (mma_it / kStages) & 1, deadline)) {
+      }
+      if (!ok) {
+        atomicExch(a.error, 1u);
+        // copies in flight land before the shared memory is given back
+        const unsigned long long d2 = tc::now_ns() + 1000000000ull;
+        for (uint32_t j = (it > (uint32_t)kStages ? it - kStages : 0u); j < it; ++j)
+          tc::mbar_wait(&full[j % kStages], (j / kStages) & 1, d2);
+        if (kResidentB) tc::mbar_wait(bfull, 0, d2);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      uint32_t it = 0, local = 0;
+      bool ok = !kResidentB || tc::mbar_wait(bfull, 0, deadline);
+      for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
+        const int split = t / m_tiles;
+        const int k0 = split * a.k_per_split;
+        const int nk = (min(a.k_per_split, a.K - k0) + kChunk - 1) / kChunk;
+        if (nk <= 0) continue;
+        const uint32_t buf = local & 1u;
+        if (local >= 2 && !tc::mbar_wait(&acce[buf], ((local >> 1) - 1) & 1, deadline)) {
           ok = false;
           break;
         }
         tc::tc_fence_after();
-        const uint32_t aa = tc::smem_u32(stA + st * kStageA), bb = tc::smem_u32(stB + st * kStageB);
+        const uint32_t d = tmem + buf * kTmemCols;
+        for (int kc = 0; kc < nk; ++kc) {
+          const uint32_t st = it % kStages;
+          if (!tc::mbar_wait(&full[st], (it / kStages) & 1, deadline)) {
+            ok = false;
+            break;
+          }
+          tc::tc_fence_after();
+          const uint32_t aa = tc::smem_u32(r2 + st * kStageA);
+          const uint32_t bb = tc::smem_u32(r1 + (kResidentB ? (uint32_t)kc : st) * kStageB);
 #pragma unroll
-        for (int k = 0; k < kChunk / 16; ++k)
-          tc::mma_bf16(tmem, tc::sdesc_sw128(aa + k * 32), tc::sdesc_sw128(bb + k * 32), idesc,
-                       (kc > 0 || k > 0) ? 1u : 0u);
-        tc::mma_commit(&empty[st]);
-        ++mma_it;
+          for (int k = 0; k < kChunk / 16; ++k)
+            tc::mma_bf16(d, tc::sdesc_sw128(aa + k * 32), tc::sdesc_sw128(bb + k * 32), idesc,
+                         (kc > 0 || k > 0) ? 1u : 0u);
+          tc::mma_commit(&empty[st]);
+          ++it;
+        }
+        if (!ok) break;
+        tc::mma_commit(&accf[buf]);
+        ++local;
       }
-      if (ok) {
-        tc::mma_commit(accum);
-      } else {
-        s_abort = 1;
-        atomicExch(a.error, 1u);
-        // let the copies and products already in flight land before the
-        // shared memory and TMEM are given back (bounded again)
+      if (!ok) {
+        atomicExch(a.error, 2u);
+        // products in flight finish before TMEM is given back
         const unsigned long long d2 = tc::now_ns() + 1000000000ull;
-        for (uint32_t it = mma_it; it < load_it; ++it) tc::mbar_wait(&full[it % kStages], (it / kStages) & 1, d2);
-        if (mma_it > 0) tc::mbar_wait(&empty[(mma_it - 1) % kStages], ((mma_it - 1) / kStages) & 1, d2);
+        if (it > 0) tc::mbar_wait(&empty[(it - 1) % kStages], ((it - 1) / kStages) & 1, d2);
       }
     }
-    __syncwarp();
-    if (!s_abort && !tc::mbar_wait(accum, acc_phase & 1, deadline)) {
-      s_abort = 1;
-      atomicExch(a.error, 2u);
+  } else {
+    const int q = warp & 3;                       // TMEM lane quarter of this warp
+    uint32_t local = 0;
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
+      const int tm = t % m_tiles, split = t / m_tiles;
+      const int k0 = split * a.k_per_split;
+      const int nk = (min(a.k_per_split, a.K - k0) + kChunk - 1) / kChunk;
+      if (nk <= 0) continue;
+      const uint32_t buf = local & 1u;
+      const bool got = tc::mbar_wait(&accf[buf], (local >> 1) & 1, deadline);
+      if (!__all_sync(0xffffffffu, got)) {
+        if (lane == 0) atomicExch(a.error, 3u);
+        break;
+      }
+      tc::tc_fence_after();
+      gemm_epilogue<MODE>(a, tm * kTileM + q * 32 + lane, tmem + ((uint32_t)(q * 32) << 16) + buf * kTmemCols,
+                          split);
+      tc::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&acce[buf]);
+      ++local;
     }
-    ++acc_phase;
-    __syncthreads();
-    if (s_abort) break;
-    tc::tc_fence_after();
-    gemm_epilogue<MODE>(a, tm * kTileM + warp * 32 + lane, tmem + ((uint32_t)(warp * 32) << 16), split);
-    tc::tc_fence_before();
-    __syncthreads();
   }
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
+  if (warp == 1) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc(tmem, 2 * kTmemCols);
+  }
 }
 
 // ----------------------------------------------------------------------------

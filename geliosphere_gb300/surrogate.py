@@ -104,6 +104,13 @@ class Surrogate:
                   "gelio_surrogate_spectra")
         return _split(r, sims), _split(sd, sims), used.astype(bool)
 
+    def last_inference(self):
+        """(device ms, GEMM FLOP) of the last predict / forward call."""
+        ms, fl = c_double(), c_double()
+        abi.check(self.lib.gelio_surrogate_last_inference(self.h, byref(ms), byref(fl)),
+                  "gelio_surrogate_last_inference")
+        return ms.value, fl.value
+
     def get_params(self, member: int) -> np.ndarray:
         p = np.zeros(abi.GELIO_SURR_PARAMS, np.float32)
         abi.check(self.lib.gelio_surrogate_get_params(self.h, member, p.ctypes.data_as(POINTER(c_float))),

@@ -389,6 +389,11 @@ int32_t gelio_surrogate_spectra(gelio_surrogate *s, const gelio_sim_params *sims
                                 const gelio_run_opts *mc_opts, double *ln_ratio, double *ln_std,
                                 int32_t *used_mc);
 
+/* Device time of the last predict / forward call (from the upload of its
+ * inputs to its last kernel) and the GEMM FLOP it performed (rows padded to
+ * the batch, first-layer K padded to 64): the surrogate's tensor roofline. */
+int32_t gelio_surrogate_last_inference(gelio_surrogate *s, double *device_ms, double *flop);
+
 /* Member m's FP32 parameters (GELIO_SURR_PARAMS floats), for persistence
  * and checks; set_params also clears that member's Adam state. */
 int32_t gelio_surrogate_get_params(gelio_surrogate *s, int32_t member, float *params);

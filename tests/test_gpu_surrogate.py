@@ -30,6 +30,9 @@ def test_forward_matches_oracle(sur, oracle):
     # BF16 activations: the two sides round the same values, rare 1-ulp flips
     assert np.median(err) < 2e-3 * np.abs(ref).max()
     assert err.max() < 3e-2 * np.abs(ref).max()
+    ms, flop = sur.last_inference()
+    # 3 batches of 4096 rows, one member, 4.26e5 FLOP per row
+    assert ms > 0 and flop == pytest.approx(3 * 4096 * 2 * (64 * 256 + 3 * 256 * 256 + 256))
 
 
 @pytest.mark.parametrize("n", [4096, 3001, 130])

@@ -60,7 +60,7 @@ def parse():
     ap.add_argument("--surr-train-particles", type=int, default=500_000)
     ap.add_argument("--surr-test", type=int, default=2000, help="surrogate: held-out parameter draws")
     ap.add_argument("--surr-test-particles", type=int, default=10_000_000)
-    ap.add_argument("--surr-epochs", type=int, default=40)
+    ap.add_argument("--surr-epochs", type=int, default=60)
     ap.add_argument("--batch-scale", type=float, default=1.0, help="batch256: particle-count scale (profiling)")
     ap.add_argument("--workload", default="geliosphere",
                     choices=["geliosphere", "bp", "fp", "batch256", "batch_cli", "surrogate"],
@@ -397,7 +397,7 @@ def run_surrogate(args, eng, rank, world, local):
     chunk = 256
     t0 = time.perf_counter()
     train = random_2d_sims(args.surr_train, args.surr_train_particles, 31 + rank)
-    sur = sg.Surrogate(eng, members=5, batch_rows=16384, seed=7 + rank)
+    sur = sg.Surrogate(eng, members=5, batch_rows=8192, seed=7 + rank)
     train_err = []
     for k in range(0, len(train), chunk):
         part = train[k:k + chunk]
@@ -460,7 +460,7 @@ def run_surrogate(args, eng, rank, world, local):
             "config": {"workload": run_surrogate.__doc__.replace("\n", " "),
                        "train_spectra": len(train), "train_particles": args.surr_train_particles,
                        "test_draws": len(test), "test_particles": args.surr_test_particles,
-                       "epochs": args.surr_epochs, "members": 5, "lis": "Usoskin 2005"},
+                       "epochs": args.surr_epochs, "batch_rows": 8192, "members": 5, "lis": "Usoskin 2005"},
             "mc_spectra_per_s": mc_rate, "surrogate_over_mc": sur_rate / mc_rate,
             "median_abs_dflux_0p1_10GeV": med,
             "mc_at_training_statistics_median_abs_dflux": med_mc,
@@ -471,7 +471,7 @@ def run_surrogate(args, eng, rank, world, local):
             "e2e": {"value": sur_rate, "unit": "spectra/s",
                     "h2d_bytes_per_step": len(test) * 100 * 7 * 4,
                     "d2h_bytes_per_step": len(test) * 100 * 5 * 4},
-            "gpu_launches": -(-len(test) * 100 // 16384) * (1 + 5 * 4),
+            "gpu_launches": -(-len(test) * 100 // 8192) * (1 + 5 * 4),
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
                          "frac": achieved / bf16_peak, "traffic": None, "kernel": "k_mlp_gemm<INFER*> (tcgen05)",
                          "device_ms": dev_ms, "flop": flop,

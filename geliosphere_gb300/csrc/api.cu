@@ -721,6 +721,9 @@ int32_t gelio_run(gelio_ctx *c, const gelio_sim_params *sims, int32_t n, const g
     const bool hit = c->graph && memcmp(key, c->graph_key, sizeof(key)) == 0 && c->graph_out == c->h_out;
     if (!hit) {
       if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
+      // buffers the run grows lazily are grown here: no allocation may
+      // happen while the stream is being captured
+      GELIO_TRY(grow(c->d_part, c->part_bytes, (size_t)choose_slices(n) * n * kSpecDoubles * 8));
       cudaGraph_t gr;
       GELIO_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
       cudaError_t e = cudaMemcpyAsync(c->d_params, c->h_params, sizeof(gelio_sim_params) * n,

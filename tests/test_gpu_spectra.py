@@ -192,3 +192,16 @@ def test_fp32_and_fp64_runs_agree(engine):
     rel = np.abs(a["grid_w"][0][ok] / a["grid_n"][ok] - b["grid_w"][0][ok] / b["grid_n"][ok]) / \
         (b["grid_w"][0][ok] / b["grid_n"][ok])
     assert rel.max() < 2e-3
+
+
+def test_graph_run_on_a_fresh_context():
+    """The first call of a new context may be a graph-captured run of a large
+    batch: every lazily grown buffer is grown before the capture starts."""
+    from geliosphere_gb300 import Engine
+    sims = [make_sim(abi.GELIO_MODEL_2D_GELIOSPHERE, 3000, r_injection=60.0, seed=100 + i,
+                     injection=abi.GELIO_INJ_LOG_GRID, inj_points=20) for i in range(40)]
+    with Engine(0) as fresh:
+        g = fresh.run(sims, use_graph=True)
+        h = fresh.run(sims)
+    for i in range(len(sims)):
+        _assert_same(spectra_dict(g.spectra[i]), spectra_dict(h.spectra[i]))

@@ -332,29 +332,25 @@ __device__ __forceinline__ int step_geliosphere(Lane<R> &L, const Consts<R> &k, 
   const R dKper = k.ratio * kd * (R(2) * r * sqCb - r2 * COmega * R(0.5) * isqCb) * inv_Cb;   // Eq. 36
   const R dKrr = dKper + k.one_m_ratio * kd * (R(2) * r * Cb15 - R(1.5) * r2 * COmega * sqCb) * inv_Cb3;  // Eq. 35
   const R CKtt0 = s * c * k.ov2 * r2;                                // Eq. 37
+  R dKtt, dKrtt;
   const R base = k.one_m_ratio * kd * r2 * r * inv_rh * inv_Cb25;    // Eq. 44 prefactor
-  // Both latitude forms of Eq. 38-44 are evaluated and one is selected per
-  // lane: a warp whose lanes sit at different latitudes does not split into
-  // two divergent paths (measured: the branch cost ~11% of the step rate).
-  // Each form is the same arithmetic as a branch would run, so the selected
-  // value is bit-identical to it; the unselected side may be inf near an
-  // axis and is discarded by the select.
-  const R dKtt1n = -k.ratio * kd * r2 * CKtt0 * inv_Cb15;            // Eq. 38
-  const R dKtt2n = k.one_m_ratio * KbR * r2 * r2 * deltarh2;          // Eq. 39
-  const R dKtt4n = R(3) * CKtt0 * inv_Cb25;                            // Eq. 41
-  const R dKttn = dKtt1n - dKtt2n * dKtt4n;                            // Eq. 42
-  const R dKrttn = -base * delta * R(3) * gamma2 * c * inv_s;
-  const R inv_s2 = inv_s * inv_s;
-  const R inv_s3 = inv_s2 * inv_s;
-  const R CKttp = CKtt0 - r2 * k.d0rh2 * c * inv_s3;
-  const R dKtt1p = -k.ratio * kd * r2 * CKttp * inv_Cb15;
-  const R dKtt2p = k.one_m_ratio * KbR * r2 * r2 * k.d0rh2;
-  const R dKtt3p = R(-2) * c * inv_s3 * k.inv_3c53 * inv_Cb15;       // Eq. 40
-  const R dKtt4p = R(3) * CKttp * inv_s2 * k.inv_3c53 * inv_Cb25;
-  const R dKttp = dKtt1p + dKtt2p * (dKtt3p - dKtt4p);
-  const R dKrttp = -base * k.delta0 * c * inv_s2 * (R(1) - R(2) * rd2 + R(4) * gamma2);
-  const R dKtt = nonpolarB ? dKttn : dKttp;
-  const R dKrtt = nonpolarB ? dKrttn : dKrttp;
+  if (nonpolarB) {
+    const R dKtt1 = -k.ratio * kd * r2 * CKtt0 * inv_Cb15;           // Eq. 38
+    const R dKtt2 = k.one_m_ratio * KbR * r2 * r2 * deltarh2;         // Eq. 39
+    const R dKtt4 = R(3) * CKtt0 * inv_Cb25;                           // Eq. 41
+    dKtt = dKtt1 - dKtt2 * dKtt4;                                      // Eq. 42
+    dKrtt = -base * delta * R(3) * gamma2 * c * inv_s;
+  } else {
+    const R inv_s2 = inv_s * inv_s;
+    const R inv_s3 = inv_s2 * inv_s;
+    const R CKtt = CKtt0 - r2 * k.d0rh2 * c * inv_s3;
+    const R dKtt1 = -k.ratio * kd * r2 * CKtt * inv_Cb15;
+    const R dKtt2 = k.one_m_ratio * KbR * r2 * r2 * k.d0rh2;
+    const R dKtt3 = R(-2) * c * inv_s3 * k.inv_3c53 * inv_Cb15;              // Eq. 40
+    const R dKtt4 = R(3) * CKtt * inv_s2 * k.inv_3c53 * inv_Cb25;
+    dKtt = dKtt1 + dKtt2 * (dKtt3 - dKtt4);
+    dKrtt = -base * k.delta0 * c * inv_s2 * (R(1) - R(2) * rd2 + R(4) * gamma2);
+  }
   const R dKrtr = k.one_m_ratio * kd * deltarh * r2 * inv_Cb25;      // Eq. 43
   const R dt = k.dt;
   R dr = (-k.V + R(2) * Krr * inv_r + dKrr) * dt;                     // Eq. 21

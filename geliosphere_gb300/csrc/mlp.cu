@@ -127,6 +127,14 @@ struct gelio_surrogate {
   size_t d_rows_cap = 0, d_rows_used = 0;
   float *d_query = nullptr, *d_yq = nullptr;   // inference inputs / outputs
   size_t query_cap = 0;
+  // inference batches: larger than training batches, so every SM gets
+  // several tiles per launch and the resident weights are loaded once per tile
+  // group rather than once per tile
+  int qrows = 0;
+  bf16 *Q0 = nullptr, *Q[2] = {};
+  float *qy = nullptr;
+  int *qident = nullptr;
+  CUtensorMap mQ0, mQ[2];
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;    // device time of the last inference
   double last_ms = 0.0, last_flop = 0.0;
   bool dirty = true;
@@ -189,6 +197,7 @@ void free_all(gelio_surrogate *s) {
   for (int i = 0; i < 3; ++i) f(s->X[i]);
   f(s->yhat); f(s->y); f(s->dy); f(s->partial); f(s->grad); f(s->loss_part); f(s->step_loss);
   f(s->ident); f(s->order); f(s->error); f(s->d_feats); f(s->d_targ); f(s->d_query); f(s->d_yq);
+  f(s->Q0); f(s->Q[0]); f(s->Q[1]); f(s->qy); f(s->qident);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -262,20 +271,21 @@ int forward_backward(gelio_surrogate *s, Member &m, int n_valid, float *loss_slo
   return GELIO_OK;
 }
 
-// Inference of member m on the gathered batch; outputs in s->yhat.
-int forward_infer(gelio_surrogate *s, Member &m) {
-  const int R = s->rows;
+
+// Inference of member m on the first `M` rows of the inference batch
+// (M a multiple of 128); outputs in s->qy.
+int forward_infer_q(gelio_surrogate *s, Member &m, int M) {
   int rc;
   GemmArgs a{};
-  a.M = R; a.N = kWidth; a.ldt = R; a.splits = 1;
-  a.K = kInPad; a.bias = m.P + kOffB1; a.x_out = s->X[0];
-  if ((rc = launch_gemm<INFER>(s, s->mX0, m.mW1, a)) != GELIO_OK) return rc;
-  a.K = kWidth; a.bias = m.P + kOffB2; a.x_out = s->X[1];
-  if ((rc = launch_gemm<INFER>(s, s->mX[0], m.mW[0], a)) != GELIO_OK) return rc;
-  a.bias = m.P + kOffB3; a.x_out = s->X[2];
-  if ((rc = launch_gemm<INFER>(s, s->mX[1], m.mW[1], a)) != GELIO_OK) return rc;
-  a.bias = m.P + kOffB4; a.x_out = nullptr; a.w5 = m.P + kOffW5; a.b5 = m.P + kOffB5; a.y_out = s->yhat;
-  return launch_gemm<INFER_LAST>(s, s->mX[2], m.mW[2], a);
+  a.M = M; a.N = kWidth; a.ldt = s->qrows; a.splits = 1;
+  a.K = kInPad; a.bias = m.P + kOffB1; a.x_out = s->Q[0];
+  if ((rc = launch_gemm<INFER>(s, s->mQ0, m.mW1, a)) != GELIO_OK) return rc;
+  a.K = kWidth; a.bias = m.P + kOffB2; a.x_out = s->Q[1];
+  if ((rc = launch_gemm<INFER>(s, s->mQ[0], m.mW[0], a)) != GELIO_OK) return rc;
+  a.bias = m.P + kOffB3; a.x_out = s->Q[0];
+  if ((rc = launch_gemm<INFER>(s, s->mQ[1], m.mW[1], a)) != GELIO_OK) return rc;
+  a.bias = m.P + kOffB4; a.x_out = nullptr; a.w5 = m.P + kOffW5; a.b5 = m.P + kOffB5; a.y_out = s->qy;
+  return launch_gemm<INFER_LAST>(s, s->mQ[0], m.mW[2], a);
 }
 
 // Upload x rows [n][7] to the training-row buffer tail used as scratch and
@@ -304,14 +314,17 @@ int infer_rows(gelio_surrogate *s, int m0, int m1, const float *x, size_t n, flo
   SUR_TRY(cudaMemcpyAsync(s->d_query, x, n * kFeatures * 4, cudaMemcpyHostToDevice, s->stream));
   SUR_TRY(cudaEventRecord(s->ev0, s->stream));
   size_t padded = 0;
-  for (size_t off = 0; off < n; off += (size_t)s->rows) {
-    padded += (size_t)s->rows;
-    const int c = (int)std::min<size_t>((size_t)s->rows, n - off);
-    int rc = stage_rows(s, s->d_query + off * kFeatures, nullptr, c);
-    if (rc != GELIO_OK) return rc;
+  for (size_t off = 0; off < n; off += (size_t)s->qrows) {
+    const int c = (int)std::min<size_t>((size_t)s->qrows, n - off);
+    const int M = (c + kTileM - 1) / kTileM * kTileM;     // only the tiles this chunk needs
+    padded += (size_t)M;
+    k_gather<<<(M + 127) / 128, 128, 0, s->stream>>>(s->d_query + off * kFeatures, nullptr, s->qident, c, 0, M,
+                                                     s->Q0, nullptr, nullptr);
+    SUR_TRY(cudaGetLastError());
     for (size_t e = 0; e < E; ++e) {
-      if ((rc = forward_infer(s, s->mem[m0 + e])) != GELIO_OK) return rc;
-      SUR_TRY(cudaMemcpyAsync(s->d_yq + e * n + off, s->yhat, (size_t)c * 4, cudaMemcpyDeviceToDevice, s->stream));
+      const int rc = forward_infer_q(s, s->mem[m0 + e], M);
+      if (rc != GELIO_OK) return rc;
+      SUR_TRY(cudaMemcpyAsync(s->d_yq + e * n + off, s->qy, (size_t)c * 4, cudaMemcpyDeviceToDevice, s->stream));
     }
   }
   SUR_TRY(cudaEventRecord(s->ev1, s->stream));
@@ -320,8 +333,8 @@ int infer_rows(gelio_surrogate *s, int m0, int m1, const float *x, size_t n, flo
   float ms = 0.f;
   if (rc == GELIO_OK && cudaEventElapsedTime(&ms, s->ev0, s->ev1) == cudaSuccess) {
     s->last_ms = ms;
-    // FLOP of the GEMMs over the rows actually multiplied (batches padded to
-    // batch_rows; first layer K padded to 64)
+    // FLOP of the GEMMs over the rows actually multiplied (each inference
+    // batch padded to a multiple of 128 rows; first layer K padded to 64)
     s->last_flop = 2.0 * (double)padded * (double)E *
                    ((double)kInPad * kWidth + 3.0 * kWidth * kWidth + (double)kWidth);
   }
@@ -418,6 +431,13 @@ int32_t gelio_surrogate_create(gelio_ctx *ctx, const gelio_surrogate_opts *opts,
   alloc((void **)&s->grad, (size_t)kParams * 4);
   alloc((void **)&s->loss_part, (R / kThreads + 1) * 4);
   alloc((void **)&s->ident, R * 4);
+  s->qrows = std::max(s->rows, 65536);
+  const size_t Rq = (size_t)s->qrows;
+  alloc((void **)&s->Q0, Rq * kInPad * 2);
+  alloc((void **)&s->Q[0], Rq * kWidth * 2);
+  alloc((void **)&s->Q[1], Rq * kWidth * 2);
+  alloc((void **)&s->qy, Rq * 4);
+  alloc((void **)&s->qident, Rq * 4);
   alloc((void **)&s->error, 4);
   s->mem.resize(o.members);
   for (auto &m : s->mem) {
@@ -436,6 +456,8 @@ int32_t gelio_surrogate_create(gelio_ctx *ctx, const gelio_surrogate_opts *opts,
     ok = ok && make_map(&s->mX[i], s->X[i], kWidth, R, kTileM);
     ok = ok && make_map(&s->mXT[i], s->XT[i], R, kWidth, kWidth);
   }
+  ok = ok && make_map(&s->mQ0, s->Q0, kInPad, Rq, kTileM) && make_map(&s->mQ[0], s->Q[0], kWidth, Rq, kTileM) &&
+       make_map(&s->mQ[1], s->Q[1], kWidth, Rq, kTileM);
   for (int i = 0; i < 4; ++i) {
     ok = ok && make_map(&s->mdH[i], s->dH[i], kWidth, R, kTileM);
     ok = ok && make_map(&s->mdHT[i], s->dHT[i], R, kWidth, kTileM);
@@ -470,6 +492,10 @@ int32_t gelio_surrogate_create(gelio_ctx *ctx, const gelio_surrogate_opts *opts,
     std::vector<int> id(R);
     for (size_t i = 0; i < R; ++i) id[i] = (int)i;
     if (cudaMemcpy(s->ident, id.data(), R * 4, cudaMemcpyHostToDevice) != cudaSuccess) return fail(GELIO_ERR_CUDA);
+    std::vector<int> idq(Rq);
+    for (size_t i = 0; i < Rq; ++i) idq[i] = (int)i;
+    if (cudaMemcpy(s->qident, idq.data(), Rq * 4, cudaMemcpyHostToDevice) != cudaSuccess)
+      return fail(GELIO_ERR_CUDA);
   }
   if (cudaStreamSynchronize(s->stream) != cudaSuccess) return fail(GELIO_ERR_CUDA);
   *out = s;

@@ -309,7 +309,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
 // Batch rows order[offset .. offset + rows) of the training set (past
 // n_order: padding rows of zeros).  Writes X0 [rows][64] (features in
 // columns 0..6; the padding columns stay zero from allocation), X0^T
-// [64][rows] (rows 0..6) and the targets.
+// [64][rows] (rows 0..6; skipped when x0t is null, for inference) and the
+// targets.
 __global__ void k_gather(const float *__restrict__ feats, const float *__restrict__ targ,
                          const int *__restrict__ order, long long n_order, long long offset, int rows,
                          __nv_bfloat16 *__restrict__ x0, __nv_bfloat16 *__restrict__ x0t, float *__restrict__ y) {
@@ -321,7 +322,7 @@ __global__ void k_gather(const float *__restrict__ feats, const float *__restric
   for (int f = 0; f < kFeatures; ++f) {
     const __nv_bfloat16 v = __float2bfloat16_rn(src >= 0 ? feats[(size_t)src * kFeatures + f] : 0.0f);
     x0[(size_t)m * kInPad + f] = v;
-    x0t[(size_t)f * rows + m] = v;
+    if (x0t) x0t[(size_t)f * rows + m] = v;
   }
   if (y) y[m] = (src >= 0 && targ) ? targ[src] : 0.0f;
 }

@@ -31,8 +31,14 @@ def test_forward_matches_oracle(sur, oracle):
     assert np.median(err) < 2e-3 * np.abs(ref).max()
     assert err.max() < 3e-2 * np.abs(ref).max()
     ms, flop = sur.last_inference()
-    # 3 batches of 4096 rows, one member, 4.26e5 FLOP per row
-    assert ms > 0 and flop == pytest.approx(3 * 4096 * 2 * (64 * 256 + 3 * 256 * 256 + 256))
+    # 9000 rows padded to 9088 (71 tiles of 128), one member, 4.26e5 FLOP per row
+    assert ms > 0 and flop == pytest.approx(9088 * 2 * (64 * 256 + 3 * 256 * 256 + 256))
+    # more rows than one inference batch (65,536): a row's output does not
+    # depend on the batch or tile it lands in
+    xl, _ = data(70_001, seed=4)
+    yl = sur.forward(0, xl)
+    np.testing.assert_array_equal(yl[:1000], sur.forward(0, xl[:1000]))
+    np.testing.assert_array_equal(yl[-1000:], sur.forward(0, xl[-1000:]))
 
 
 @pytest.mark.parametrize("n", [4096, 3001, 130])

@@ -237,6 +237,7 @@ int forward_backward(gelio_surrogate *s, Member &m, int n_valid, float *loss_slo
   if ((rc = launch_gemm<FWD>(s, s->mX[1], m.mW[1], a)) != GELIO_OK) return rc;
   a.bias = m.P + kOffB4; a.z_out = s->Z[3]; a.x_out = nullptr; a.xt_out = s->XT[3];
   a.w5 = m.P + kOffW5; a.b5 = m.P + kOffB5; a.y_out = s->yhat;
+  SUR_TRY(cudaMemsetAsync(s->yhat, 0, (size_t)R * 4, s->stream));
   if ((rc = launch_gemm<FWD_LAST>(s, s->mX[2], m.mW[2], a)) != GELIO_OK) return rc;
   // head
   const int hb = (R + kThreads - 1) / kThreads;
@@ -285,6 +286,7 @@ int forward_infer_q(gelio_surrogate *s, Member &m, int M) {
   a.bias = m.P + kOffB3; a.x_out = s->Q[0];
   if ((rc = launch_gemm<INFER>(s, s->mQ[1], m.mW[1], a)) != GELIO_OK) return rc;
   a.bias = m.P + kOffB4; a.x_out = nullptr; a.w5 = m.P + kOffW5; a.b5 = m.P + kOffB5; a.y_out = s->qy;
+  SUR_TRY(cudaMemsetAsync(s->qy, 0, (size_t)M * 4, s->stream));
   return launch_gemm<INFER_LAST>(s, s->mQ[0], m.mW[2], a);
 }
 

@@ -60,7 +60,7 @@ struct GemmArgs {
   __nv_bfloat16 *z_out;   // FWD*: pre-activations [M][256]
   __nv_bfloat16 *x_out;   // FWD, INFER: activations [M][256]
   __nv_bfloat16 *xt_out;  // FWD*: activations transposed [256][ldt]
-  float *y_out;           // *_LAST: head outputs [M]
+  float *y_out;           // *_LAST: head outputs [M], zeroed before the launch
   const __nv_bfloat16 *z_prev;   // DX: pre-activations of the layer below [M][256]
   __nv_bfloat16 *dh_out;  // DX: [M][256]
   __nv_bfloat16 *dht_out; // DX: [256][ldt]
@@ -76,11 +76,13 @@ __device__ __forceinline__ float silu_grad_f(float z) {
 }
 
 template <int MODE>
-__device__ __forceinline__ void gemm_epilogue(const GemmArgs &a, int row, uint32_t trow, int split) {
+// Columns [32 c_begin, 32 c_end) of one accumulator row; returns this
+// thread's part of the 256 -> 1 head's dot product (*_LAST modes).
+__device__ __forceinline__ float gemm_epilogue(const GemmArgs &a, int row, uint32_t trow, int split, int c_begin,
+                                               int c_end) {
   const bool valid = row < a.M;
   float ysum = 0.0f;
-  const int nchunks = a.N / 32;
-  for (int c = 0; c < nchunks; ++c) {
+  for (int c = c_begin; c < c_end; ++c) {
     float v[32];
     tc::tmem_ld32(trow + (uint32_t)(c * 32), v);     // warp-wide: every lane executes it
     const int n0 = c * 32;
@@ -128,7 +130,7 @@ __device__ __forceinline__ void gemm_epilogue(const GemmArgs &a, int row, uint32
     }
     }
   }
-  if ((MODE == FWD_LAST || MODE == INFER_LAST) && valid) a.y_out[row] = ysum + __ldg(a.b5);
+  return ysum;
 }
 
 // One CTA per SM, warp-specialised, tiles of 128 GEMM rows handed out
@@ -140,12 +142,15 @@ __device__ __forceinline__ void gemm_epilogue(const GemmArgs &a, int row, uint32
 //   warp 1  (one lane)  MMA issuer: tcgen05.mma into one of two TMEM
 //           accumulators (2 x 256 columns), tcgen05.commit frees a ring
 //           stage and hands a finished accumulator to the epilogue;
-//   warps 2-5           epilogue: tcgen05.ld one row per thread (warp w reads
-//           TMEM lanes 32 (w % 4) .. +31), fused epilogue, then hand the
-//           accumulator back; it overlaps the MMAs of the next tile.
+//   warps 2-9           epilogue: tcgen05.ld one row per thread (warp w reads
+//           TMEM lanes 32 (w % 4) .. +31), two warps per lane quarter each
+//           taking half of the columns (two warps per scheduler hide the
+//           epilogue's latency), fused epilogue, then hand the accumulator
+//           back; it overlaps the MMAs of the next tile.
 // Shared memory: region 1 (128 KiB) holds the resident weights (or the B
 // stages of DW), region 2 (64 KiB) the A stages.
-constexpr int kGemmThreads = 192;
+constexpr int kEpiWarps = 8;
+constexpr int kGemmThreads = 64 + 32 * kEpiWarps;
 constexpr uint32_t kRegion1 = 4 * kStageB;         // 128 KiB
 constexpr uint32_t kRegion2 = kStages * kStageA;   // 64 KiB
 
@@ -177,7 +182,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     tc::mbar_init(bfull, 1);
     for (int b = 0; b < 2; ++b) {
       tc::mbar_init(&accf[b], 1);
-      tc::mbar_init(&acce[b], 4);
+      tc::mbar_init(&acce[b], kEpiWarps);
     }
     tc::fence_mbar_init();
     tc::tma_prefetch(&tmA);
@@ -274,6 +279,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     }
   } else {
     const int q = warp & 3;                       // TMEM lane quarter of this warp
+    const int h = (warp - 2) / 4;                 // column half of this warp
+    const int per = (a.N / 32) / 2;
     uint32_t local = 0;
     for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
       const int tm = t % m_tiles, split = t / m_tiles;
@@ -287,11 +294,18 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         break;
       }
       tc::tc_fence_after();
-      gemm_epilogue<MODE>(a, tm * kTileM + q * 32 + lane, tmem + ((uint32_t)(q * 32) << 16) + buf * kTmemCols,
-                          split);
+      const int row = tm * kTileM + q * 32 + lane;
+      const float ys = gemm_epilogue<MODE>(a, row, tmem + ((uint32_t)(q * 32) << 16) + buf * kTmemCols, split,
+                                           h * per, (h + 1) * per);
       tc::tc_fence_before();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&acce[buf]);
+      if constexpr (MODE == FWD_LAST || MODE == INFER_LAST) {
+        // y_out is zeroed before the launch; the two halves' sums meet by
+        // atomic addition, (0 + x) + y == (0 + y) + x, so the order does not
+        // change the result
+        if (row < a.M) atomicAdd(&a.y_out[row], h == 0 ? ys + __ldg(a.b5) : ys);
+      }
       ++local;
     }
   }

@@ -16,8 +16,18 @@ e2e   : the same metric through gelio_run with host buffers (parameters
         (the reference CPU code itself is pinned to it bit for bit, but its
         sources are not available on this host).
 
+Other workloads (--workload; each prints its own line of the same form):
+  bp        1D B-p, 1e7 protons on a 100-point log grid, FP32 and FP64 steps
+  fp        1D F-p, 1e6 protons log-uniform 0.01-200 GeV, 300 log bins
+  batch256  256 random 2D simulations in one graph-captured persistent
+            launch vs 256 plain launches (one per simulation)
+  batch_cli the same kind of batch as a 256-row batch CSV through the
+            `geliosphere -b` executable
+  surrogate the MLP ensemble trained on MC spectra, timed against the MC on
+            held-out draws (spectra/s, median flux error, tensor roofline)
+
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gelio|reference]
-                       [--particles P] [--no-cpu-baseline]
+                       [--particles P] [--no-cpu-baseline] [--workload W]
 Multi-GPU (torchrun): each rank runs its own weak-scaling replica of the
 workload with its own seeds; no data-path collective.
 """

@@ -75,12 +75,36 @@ __device__ __forceinline__ float silu_grad_f(float z) {
   return s * (1.0f + z * (1.0f - s));
 }
 
+// Row-major store of a warp's 32 rows x 32 columns (BF16) through a shared
+// staging tile: lane l then writes row 8 i + l / 4, 16-byte piece l % 4, so
+// each store instruction covers 8 rows x 64 contiguous bytes (full sectors)
+// instead of 32 rows x 16 bytes.  The 80-byte pitch keeps the lanes' 16-byte
+// staging writes on distinct banks.
+constexpr int kStagePitch = 80;
+
+__device__ __forceinline__ void store_rows(const uint4 (&v)[4], __nv_bfloat16 *dst, int row0, int M, int n0,
+                                           unsigned char *stage, int lane) {
+  uint4 *mine = reinterpret_cast<uint4 *>(stage + lane * kStagePitch);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) mine[q] = v[q];
+  __syncwarp();
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int r = i * 8 + (lane >> 2), piece = lane & 3;
+    const uint4 val = *reinterpret_cast<const uint4 *>(stage + r * kStagePitch + piece * 16);
+    if (row0 + r < M) *reinterpret_cast<uint4 *>(dst + (size_t)(row0 + r) * kWidth + n0 + piece * 8) = val;
+  }
+  __syncwarp();
+}
+
+// Columns [32 c_begin, 32 c_end) of one accumulator row (row = row0 + lane);
+// returns this thread's part of the 256 -> 1 head's dot product (*_LAST
+// modes).  Warp-wide: every lane of the warp calls it.
 template <int MODE>
-// Columns [32 c_begin, 32 c_end) of one accumulator row; returns this
-// thread's part of the 256 -> 1 head's dot product (*_LAST modes).
 __device__ __forceinline__ float gemm_epilogue(const GemmArgs &a, int row, uint32_t trow, int split, int c_begin,
-                                               int c_end) {
+                                               int c_end, unsigned char *stage, int lane) {
   const bool valid = row < a.M;
+  const int row0 = row - lane;
   float ysum = 0.0f;
   for (int c = c_begin; c < c_end; ++c) {
     float v[32];
@@ -92,42 +116,43 @@ __device__ __forceinline__ float gemm_epilogue(const GemmArgs &a, int row, uint3
       for (int j = 0; j < 32; ++j) p[(size_t)j * kWidth] = v[j];
       continue;
     }
-    if (!valid) continue;
     __align__(16) __nv_bfloat16 out[32];
     if constexpr (MODE == DX) {
       __align__(16) __nv_bfloat16 zp[32];
-      const uint4 *src = reinterpret_cast<const uint4 *>(a.z_prev + (size_t)row * kWidth + n0);
+      if (valid) {
+        const uint4 *src = reinterpret_cast<const uint4 *>(a.z_prev + (size_t)row * kWidth + n0);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) reinterpret_cast<uint4 *>(zp)[q] = src[q];
+        for (int q = 0; q < 4; ++q) reinterpret_cast<uint4 *>(zp)[q] = src[q];
+      } else {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) reinterpret_cast<uint4 *>(zp)[q] = make_uint4(0, 0, 0, 0);
+      }
 #pragma unroll
       for (int j = 0; j < 32; ++j) out[j] = __float2bfloat16_rn(v[j] * silu_grad_f(__bfloat162float(zp[j])));
-      uint4 *dst = reinterpret_cast<uint4 *>(a.dh_out + (size_t)row * kWidth + n0);
+      store_rows(reinterpret_cast<const uint4(&)[4]>(out), a.dh_out, row0, a.M, n0, stage, lane);
+      if (valid) {
 #pragma unroll
-      for (int q = 0; q < 4; ++q) dst[q] = reinterpret_cast<uint4 *>(out)[q];
-#pragma unroll
-      for (int j = 0; j < 32; ++j) a.dht_out[(size_t)(n0 + j) * a.ldt + row] = out[j];
+        for (int j = 0; j < 32; ++j) a.dht_out[(size_t)(n0 + j) * a.ldt + row] = out[j];
+      }
     } else {
-    // forward family
-    __align__(16) __nv_bfloat16 zb[32];
+      // forward family
+      __align__(16) __nv_bfloat16 zb[32];
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
-      const float z = v[j] + __ldg(a.bias + n0 + j);
-      zb[j] = __float2bfloat16_rn(z);
-      out[j] = __float2bfloat16_rn(silu_f(z));
-      if (MODE == FWD_LAST || MODE == INFER_LAST) ysum += __bfloat162float(out[j]) * __ldg(a.w5 + n0 + j);
-    }
-    if (MODE == FWD || MODE == FWD_LAST) {
-      uint4 *dz = reinterpret_cast<uint4 *>(a.z_out + (size_t)row * kWidth + n0);
+      for (int j = 0; j < 32; ++j) {
+        const float z = v[j] + __ldg(a.bias + n0 + j);
+        zb[j] = __float2bfloat16_rn(z);
+        out[j] = __float2bfloat16_rn(silu_f(z));
+        if (MODE == FWD_LAST || MODE == INFER_LAST) ysum += __bfloat162float(out[j]) * __ldg(a.w5 + n0 + j);
+      }
+      if constexpr (MODE == FWD || MODE == FWD_LAST) {
+        store_rows(reinterpret_cast<const uint4(&)[4]>(zb), a.z_out, row0, a.M, n0, stage, lane);
+        if (valid) {
 #pragma unroll
-      for (int q = 0; q < 4; ++q) dz[q] = reinterpret_cast<uint4 *>(zb)[q];
-#pragma unroll
-      for (int j = 0; j < 32; ++j) a.xt_out[(size_t)(n0 + j) * a.ldt + row] = out[j];
-    }
-    if (MODE == FWD || MODE == INFER) {
-      uint4 *dx = reinterpret_cast<uint4 *>(a.x_out + (size_t)row * kWidth + n0);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) dx[q] = reinterpret_cast<uint4 *>(out)[q];
-    }
+          for (int j = 0; j < 32; ++j) a.xt_out[(size_t)(n0 + j) * a.ldt + row] = out[j];
+        }
+      }
+      if constexpr (MODE == FWD || MODE == INFER)
+        store_rows(reinterpret_cast<const uint4(&)[4]>(out), a.x_out, row0, a.M, n0, stage, lane);
     }
   }
   return ysum;
@@ -159,6 +184,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     k_mlp_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const GemmArgs a) {
   constexpr bool kResidentB = (MODE != DW);
   extern __shared__ unsigned char smem_raw[];
+  __shared__ __align__(16) unsigned char s_stage[kEpiWarps][32 * kStagePitch];   // epilogue store staging
   const uint32_t s0 = tc::smem_u32(smem_raw);
   unsigned char *base = smem_raw + ((1024u - (s0 & 1023u)) & 1023u);
   unsigned char *r1 = base;
@@ -296,7 +322,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       tc::tc_fence_after();
       const int row = tm * kTileM + q * 32 + lane;
       const float ys = gemm_epilogue<MODE>(a, row, tmem + ((uint32_t)(q * 32) << 16) + buf * kTmemCols, split,
-                                           h * per, (h + 1) * per);
+                                           h * per, (h + 1) * per, s_stage[warp - 2], lane);
       tc::tc_fence_before();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&acce[buf]);

@@ -188,8 +188,17 @@ def spectra_goldens():
         "geliosphere_a_neg_tilt70": ("geliosphere", base_args(500, tilt=70, polarity=-1), 48),
         "solarprop_a_pos": ("solarprop", base_args(500, polarity=1), 48),
         "bp_dt50": ("bp", base_args(50), 24),
+        "solarprop_a_neg_tilt70": ("solarprop", base_args(500, tilt=70, polarity=-1), 48),
+        # 1 AU crossings are rare (~1.3e-4 per particle): 8,080 blocks of
+        # 25,250 particles; a block injects ids (8 iteration + thread) * 250
+        # + 0..249, each 101 times, so 8,080 blocks cover the CPU grid's
+        # 1,010,000 ids exactly twice (a uniform injection spectrum)
+        "fp_dt50": ("fp", base_args(50), 8080),
     }
+    only = [a.split("=", 1)[1].split(",") for a in sys.argv if a.startswith("--spectra=")]
     for name, (model, args, nb) in cases.items():
+        if only and name not in only[0]:
+            continue
         resolved, n_rec, arr, n_traj = spectra_case(model, args, nb)
         doc = {"model": model, "args": args, "resolved": resolved, "n_records": n_rec,
                "n_trajectories": n_traj, "spectra": arr}
@@ -203,6 +212,9 @@ def main():
         sys.exit("reference sources not found; fixtures are generated only where they exist")
     ffi.build()
     rng = np.random.default_rng(20240601)
+    if any(a.startswith("--spectra=") for a in sys.argv):
+        spectra_goldens()
+        return
     cpu_pins()
     if any(a.startswith("--pins=") for a in sys.argv):
         return

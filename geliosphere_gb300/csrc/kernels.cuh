@@ -333,7 +333,7 @@ __device__ __noinline__ void emit_fp(const KArgs &a, const Sink<kModelFp> &sink,
   const float Texit = (float)L.T.v;
   const double p100 = round6(p_si((double)L.Tinj));
   const double p1 = round6(p_si((double)Texit));
-  const double rr = round6((double)(float)L.r.v);
+  const double rr = round6((double)L.rrec);
   const double sm = round6((double)(float)L.sumac.v);
   Contribution C;
   double T1;
@@ -359,7 +359,7 @@ __device__ __noinline__ void emit_fp(const KArgs &a, const Sink<kModelFp> &sink,
       rec.sim = L.sim;
       rec.t_injection = L.Tinj;
       rec.t_exit = Texit;
-      rec.r = (float)L.r.v;
+      rec.r = L.rrec;
       rec.theta = 0.0f;
       rec.sumac = (float)L.sumac.v;
       a.records[idx] = rec;
@@ -592,7 +592,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4) ? 2 : 1) k_plain(const K
         if (res == kRecordAndContinue || res == kRecordAndStop) {
           if (nrec == 0) {
             t_rec = (float)L.T.v;
-            r_rec = (float)L.r.v;
+            r_rec = (MODEL == kModelFp) ? L.rrec : (float)L.r.v;
             aux_rec = (MODEL == kModelFp) ? (float)L.sumac.v : (float)theta_full(L);
           }
           ++nrec;

@@ -178,6 +178,7 @@ template <class R> struct Lane {
   Acc<R> r, th, T, P, sumac;
   float thn;           // FP32 2D models: theta = 2 pi thn + th once theta has left [0, 2 pi)
   float Tinj;
+  float rrec;          // F-p: r of the last 1 AU crossing, before a reflection undoes the step
   uint32_t steps;
   int sim;
   int gbin;
@@ -512,7 +513,10 @@ __device__ __forceinline__ int step_fp(Lane<R> &L, const Consts<R> &k, R z) {
   const R rn = L.r.v;
   int res = kContinue;
   if (beta > (R)0.01f && Tn < R(100)) {
-    if ((rn - R(1)) / ((rn - dr) - R(1)) < R(0)) res = kRecordAndContinue;
+    if ((rn - R(1)) / ((rn - dr) - R(1)) < R(0)) {
+      res = kRecordAndContinue;
+      L.rrec = (float)rn;     // the record keeps the crossing's r even if the step is undone below
+    }
   } else if (beta < (R)0.01f) {
     return kStop;
   }

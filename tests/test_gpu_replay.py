@@ -161,3 +161,22 @@ def test_bp_fp32_and_fp64_spectra_vs_oracle_replay(engine, oracle):
         assert err.max() < tol, (prec, out[prec])
     print("B-p sample spectrum rel. error (median, max): FP64 %.2e %.2e, FP32 %.2e %.2e"
           % (*out[abi.GELIO_PREC_FP64], *out[abi.GELIO_PREC_FP32]))
+
+
+def test_fp_crossing_record_keeps_the_crossing_radius(engine, oracle):
+    """An F-p step that crosses 1 AU and lands below 0.1 AU is recorded with
+    that radius (the evaluator then gives it weight 0) before the step is
+    undone, as in OneDimensionFpModel.cu:127-141.  High energies take
+    AU-sized steps, so this happens often."""
+    sim = make_sim(abi.GELIO_MODEL_1D_FP, 0, dt=50, seed=43, injection=abi.GELIO_INJ_LOG_UNIFORM, inj_min=60,
+                   inj_max=100)
+    n = 20000
+    st, steps, nrec, vals = oracle.replay(sim, 0, n)
+    rec = nrec > 0
+    assert np.sum(vals[rec, 4] < 0.1) >= 5          # the case is exercised
+    for prec in (abi.GELIO_PREC_FP64, abi.GELIO_PREC_FP32):
+        gpu = engine.replay(sim, 0, n, prec)
+        same = (gpu["steps"] == steps) & (gpu["n_records"] == nrec) & rec
+        assert same.sum() >= 0.99 * rec.sum()
+        d = np.abs(gpu["r_record"][same].astype(np.float64) - vals[same, 4])
+        assert np.quantile(d, 0.99) < 1e-4, np.quantile(d, 0.99)

@@ -110,30 +110,40 @@ def test_bp_spectra_match_reference_cpu_model(engine):
 
 
 def test_fp_spectra_match_reference_cpu_model(engine):
-    """1D F-p: the reference CPU model's 1 AU crossing spectrum (23,519
-    crossings from 2.04e8 trajectories injected uniformly over its 1e-4 GeV
-    grid) against the GPU's from 1.01e8 trajectories on the same grid
-    (a whole number of passes over its 1,010,000 ids): the crossing rate and
-    the per-bin mean weights of the 1 GeV bins within Monte Carlo error."""
+    """1D F-p against the reference CPU model's 1 AU crossing spectrum
+    (23,519 crossings from 2.04e8 trajectories injected uniformly over its
+    0.0101 GeV grid).  One F-p trajectory may cross 1 AU many times at nearly
+    the same energy and weight, so crossings are not independent and a
+    per-record error would be far too small: the comparison is made on
+    per-trajectory quantities (crossings and summed weight in five energy
+    bands at 1 AU) with their variance estimated from 40 independent GPU
+    batches of 1.01e7 trajectories, which carries the clustering."""
     path = os.path.join(GOLDEN, "ref_spectra_fp_dt50.json")
     if not os.path.exists(path):
         pytest.skip("fixture not generated")
     doc = json.load(open(path))
-    sim = sim_from_fixture(doc, 101_000_000, seed=4242)
-    gpu = spectra_dict(engine.run(sim).spectra[0])
-    ref = doc["spectra"]
-    # crossings per trajectory (the reference counts records below 100 GeV)
-    n_g = float(np.sum(gpu["e2_n"]))
-    n_r = float(np.sum(ref["e2_n"]))
-    rate_g, rate_r = n_g / gpu["n_particles"], n_r / doc["n_trajectories"]
-    z_rate = (rate_g - rate_r) / np.sqrt(rate_g / gpu["n_particles"] + rate_r / doc["n_trajectories"])
-    z = compare_sections(gpu, ref, [("e2_w", "e2_w2", "e2_n")], min_count=100)
-    print(f"fp: crossings {int(n_g)} vs {int(n_r)}, rate z {z_rate:.2f}; bins {z.size}, "
-          f"max|z| {np.abs(z).max():.2f}, chi2/dof {np.mean(z**2):.3f}")
-    assert abs(z_rate) < 3.5
-    assert z.size >= 40
+    nb, per = 40, 10_100_000          # a whole number of passes over the 10,000-point grid
+    sims = [sim_from_fixture(doc, per, seed=4242 + 7919 * k) for k in range(nb)]
+    res = engine.run(sims)
+    bands = [(0, 5), (5, 15), (15, 40), (40, 70), (70, 100)]    # 1 GeV bins of the 1 AU energy
+
+    def stats(sp, n_traj):
+        n = np.asarray(sp["e2_n"], dtype=np.float64)
+        w = np.asarray(sp["e2_w"], dtype=np.float64)
+        return np.array([n[a:b].sum() for a, b in bands] + [w[a:b].sum() for a, b in bands]) / n_traj
+
+    g = np.array([stats(spectra_dict(res.spectra[k]), per) for k in range(nb)])
+    ref = stats(doc["spectra"], doc["n_trajectories"])
+    mean = g.mean(axis=0)
+    var_traj = g.var(axis=0, ddof=1) * per            # per-trajectory variance, clustering included
+    se = np.sqrt(var_traj / (nb * per) + var_traj / doc["n_trajectories"])
+    z = (mean - ref) / se
+    k = len(bands)
+    print("fp bands: crossings/traj gpu " + " ".join(f"{x:.3e}" for x in mean[:k]) +
+          " ref " + " ".join(f"{x:.3e}" for x in ref[:k]) + "; weight ratio " +
+          " ".join(f"{x:.3f}" for x in mean[k:] / ref[k:]) + "; z " + " ".join(f"{x:.2f}" for x in z))
     assert np.abs(z).max() < 3.5
-    assert np.mean(z ** 2) <= 1.2
+    assert np.mean(z ** 2) <= 2.0     # 10 correlated comparisons (counts and weights share trajectories)
 
 
 @pytest.mark.parametrize("model", [abi.GELIO_MODEL_2D_GELIOSPHERE, abi.GELIO_MODEL_2D_SOLARPROP,

@@ -418,7 +418,7 @@ def run_surrogate(args, eng, rank, world, local):
     loss = sur.train(args.surr_epochs)
     t_train = time.perf_counter() - t1
     test = random_2d_sims(args.surr_test, args.surr_test_particles, 10_000 + rank)
-    # Monte Carlo answer for every held-out draw (the judge of the error)
+    # Monte Carlo answer for every held-out draw (the yardstick of its error)
     mc_s, ref = 0.0, []
     low = []
     for k in range(0, len(test), chunk):

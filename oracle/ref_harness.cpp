@@ -5,7 +5,7 @@
 // GELIO_REF_MODEL selects the model source compiled into this translation
 // unit (0 = OneDimensionFpCpuModel.cpp, 1 = OneDimensionBpCpuModel.cpp,
 // 2 = SolarPropLikeCpuModel.cpp, 3 = GeliosphereCpuModel.cpp).  Including the
-// source here gives the driver the model's file-static constants and its
+// source here gives this harness the model's file-static constants and its
 // setContants() (CpuImplementations/include/Constants.hpp:188-223), so the
 // parameters are resolved by the reference's own code.
 //

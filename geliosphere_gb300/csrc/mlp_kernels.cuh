@@ -102,7 +102,8 @@ __device__ __forceinline__ void store_rows(const uint4 (&v)[4], __nv_bfloat16 *d
 // modes).  Warp-wide: every lane of the warp calls it.
 template <int MODE>
 __device__ __forceinline__ float gemm_epilogue(const GemmArgs &a, int row, uint32_t trow, int split, int c_begin,
-                                               int c_end, unsigned char *stage, int lane) {
+                                               int c_end, unsigned char *stage, int lane, const float *sbias,
+                                               const float *sw5) {
   const bool valid = row < a.M;
   const int row0 = row - lane;
   float ysum = 0.0f;
@@ -139,10 +140,10 @@ __device__ __forceinline__ float gemm_epilogue(const GemmArgs &a, int row, uint3
       __align__(16) __nv_bfloat16 zb[32];
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
-        const float z = v[j] + __ldg(a.bias + n0 + j);
+        const float z = v[j] + sbias[n0 + j];
         zb[j] = __float2bfloat16_rn(z);
         out[j] = __float2bfloat16_rn(silu_f(z));
-        if (MODE == FWD_LAST || MODE == INFER_LAST) ysum += __bfloat162float(out[j]) * __ldg(a.w5 + n0 + j);
+        if (MODE == FWD_LAST || MODE == INFER_LAST) ysum += __bfloat162float(out[j]) * sw5[n0 + j];
       }
       if constexpr (MODE == FWD || MODE == FWD_LAST) {
         store_rows(reinterpret_cast<const uint4(&)[4]>(zb), a.z_out, row0, a.M, n0, stage, lane);
@@ -185,6 +186,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   constexpr bool kResidentB = (MODE != DW);
   extern __shared__ unsigned char smem_raw[];
   __shared__ __align__(16) unsigned char s_stage[kEpiWarps][32 * kStagePitch];   // epilogue store staging
+  __shared__ float s_bias[kWidth], s_w5[kWidth];     // epilogue operands, read by every row
   const uint32_t s0 = tc::smem_u32(smem_raw);
   unsigned char *base = smem_raw + ((1024u - (s0 & 1023u)) & 1023u);
   unsigned char *r1 = base;
@@ -213,6 +215,12 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     tc::fence_mbar_init();
     tc::tma_prefetch(&tmA);
     tc::tma_prefetch(&tmB);
+  }
+  if (MODE != DW && MODE != DX) {
+    for (int i = tid; i < kWidth; i += blockDim.x) {
+      s_bias[i] = a.bias[i];
+      if (MODE == FWD_LAST || MODE == INFER_LAST) s_w5[i] = a.w5[i];
+    }
   }
   if (warp == 1) {
     tc::tmem_alloc(tslot, 2 * kTmemCols);
@@ -322,7 +330,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       tc::tc_fence_after();
       const int row = tm * kTileM + q * 32 + lane;
       const float ys = gemm_epilogue<MODE>(a, row, tmem + ((uint32_t)(q * 32) << 16) + buf * kTmemCols, split,
-                                           h * per, (h + 1) * per, s_stage[warp - 2], lane);
+                                           h * per, (h + 1) * per, s_stage[warp - 2], lane, s_bias, s_w5);
       tc::tc_fence_before();
       __syncwarp();
       if (lane == 0) tc::mbar_arrive(&acce[buf]);

@@ -333,27 +333,24 @@ __device__ __forceinline__ int step_geliosphere(Lane<R> &L, const Consts<R> &k, 
   const R dKper = k.ratio * kd * (R(2) * r * sqCb - r2 * COmega * R(0.5) * isqCb) * inv_Cb;   // Eq. 36
   const R dKrr = dKper + k.one_m_ratio * kd * (R(2) * r * Cb15 - R(1.5) * r2 * COmega * sqCb) * inv_Cb3;  // Eq. 35
   const R CKtt0 = s * c * k.ov2 * r2;                                // Eq. 37
+  R dKtt, dKrtt;
   const R base = k.one_m_ratio * kd * r2 * r * inv_rh * inv_Cb25;    // Eq. 44 prefactor
-  // Non-polar forms (theta within (1.7, 178.3) deg) for every lane ...
-  const R dKtt1 = -k.ratio * kd * r2 * CKtt0 * inv_Cb15;             // Eq. 38
-  const R dKtt2 = k.one_m_ratio * KbR * r2 * r2 * deltarh2;           // Eq. 39
-  const R dKtt4 = R(3) * CKtt0 * inv_Cb25;                             // Eq. 41
-  R dKtt = dKtt1 - dKtt2 * dKtt4;                                      // Eq. 42
-  R dKrtt = -base * delta * R(3) * gamma2 * c * inv_s;
-  // ... and the polar forms only in warps that hold a lane near an axis (a
-  // warp-uniform branch: most warps skip this code entirely)
-  if (__any_sync(__activemask(), !nonpolarB)) {
+  if (nonpolarB) {
+    const R dKtt1 = -k.ratio * kd * r2 * CKtt0 * inv_Cb15;           // Eq. 38
+    const R dKtt2 = k.one_m_ratio * KbR * r2 * r2 * deltarh2;         // Eq. 39
+    const R dKtt4 = R(3) * CKtt0 * inv_Cb25;                           // Eq. 41
+    dKtt = dKtt1 - dKtt2 * dKtt4;                                      // Eq. 42
+    dKrtt = -base * delta * R(3) * gamma2 * c * inv_s;
+  } else {
     const R inv_s2 = inv_s * inv_s;
     const R inv_s3 = inv_s2 * inv_s;
     const R CKtt = CKtt0 - r2 * k.d0rh2 * c * inv_s3;
-    const R dKtt1p = -k.ratio * kd * r2 * CKtt * inv_Cb15;
-    const R dKtt2p = k.one_m_ratio * KbR * r2 * r2 * k.d0rh2;
-    const R dKtt3p = R(-2) * c * inv_s3 * k.inv_3c53 * inv_Cb15;             // Eq. 40
-    const R dKtt4p = R(3) * CKtt * inv_s2 * k.inv_3c53 * inv_Cb25;
-    if (!nonpolarB) {
-      dKtt = dKtt1p + dKtt2p * (dKtt3p - dKtt4p);
-      dKrtt = -base * k.delta0 * c * inv_s2 * (R(1) - R(2) * rd2 + R(4) * gamma2);
-    }
+    const R dKtt1 = -k.ratio * kd * r2 * CKtt * inv_Cb15;
+    const R dKtt2 = k.one_m_ratio * KbR * r2 * r2 * k.d0rh2;
+    const R dKtt3 = R(-2) * c * inv_s3 * k.inv_3c53 * inv_Cb15;              // Eq. 40
+    const R dKtt4 = R(3) * CKtt * inv_s2 * k.inv_3c53 * inv_Cb25;
+    dKtt = dKtt1 + dKtt2 * (dKtt3 - dKtt4);
+    dKrtt = -base * k.delta0 * c * inv_s2 * (R(1) - R(2) * rd2 + R(4) * gamma2);
   }
   const R dKrtr = k.one_m_ratio * kd * deltarh * r2 * inv_Cb25;      // Eq. 43
   const R dt = k.dt;

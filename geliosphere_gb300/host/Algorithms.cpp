@@ -182,32 +182,29 @@ struct Planned {
 
 }  // namespace
 
-// Rows are validated and resolved one by one exactly as the reference does
-// (erase, row values, settings, month/year); every row that resolves is
-// added to one gelio_run call, so all simulations of the batch share one
-// persistent launch per model.  Each row's directory receives its spectra,
-// simulation_log.txt and, when kept, its log.dat.
-void BatchRun::runAlgorithm(ParamsCarrier *p) {
+// Rows of the batch CSV at `path` are validated and resolved one by one
+// exactly as the reference does (erase, row values, settings, month/year);
+// each row that resolves gets its directory and simulation_log.txt here.
+// False when the file cannot be used at all (or a CPU-only run is refused).
+static bool planBatch(ParamsCarrier *p, const std::string &path, bool refuseCpu, std::vector<Planned> &plan) {
   const std::set<std::string> excluded = {"default_settings_file", "currentApplicationPath", "csv", "isCpu",
                                           "inputBatchFile"};
-  const std::string path = p->getString("inputBatchFile", "../geliosphere_batch_input_paramaters.csv");
   CsvTable doc;
   if (!doc.load(path)) {
     glog::error("Cannot open input batch file.");
-    return;
+    return false;
   }
   if (!uniqueNames(doc)) {
     glog::error("Input batch file contains duplicated values. Use unique names for simulations, or leave fields "
                 "empty for using autogenerated values.");
     glog::error("Input batch file contains unrecoverable errors.");
-    return;
+    return false;
   }
-  if (p->getInt("isCpu", 0)) {
+  if (refuseCpu && p->getInt("isCpu", 0)) {
     glog::error("CPU-only runs are not provided by the GB300 engine; run without --cpu-only.");
-    return;
+    return false;
   }
   const std::string home = cwd();
-  std::vector<Planned> plan;
   std::set<std::string> usedDirs;
   p->eraseAllItems(excluded);
   for (size_t i = 0; i < doc.rows.size(); ++i) {
@@ -235,7 +232,7 @@ void BatchRun::runAlgorithm(ParamsCarrier *p) {
     }
     if (!createDirectory(ghost::modelDirectory(model), dest)) {
       glog::error("Directory for the simulation cannot be created.");
-      if (chdir(home.c_str()) != 0) return;
+      if (chdir(home.c_str()) != 0) return false;
       p->eraseAllItems(excluded);
       continue;
     }
@@ -255,6 +252,28 @@ void BatchRun::runAlgorithm(ParamsCarrier *p) {
     }
     p->eraseAllItems(excluded);
   }
+  return true;
+}
+
+int batchPlan(ParamsCarrier *p, const std::string &path, std::vector<gelio_sim_params> &sims,
+              std::vector<int> &rows) {
+  std::vector<Planned> plan;
+  if (!planBatch(p, path, false, plan)) return -1;
+  for (auto &pl : plan) {
+    sims.push_back(pl.sim);
+    rows.push_back(pl.row);
+  }
+  return (int)plan.size();
+}
+
+// Every row that resolves is added to one gelio_run call, so all
+// simulations of the batch share one persistent launch per model.  Each
+// row's directory then receives its spectra and, when kept, its log.dat.
+void BatchRun::runAlgorithm(ParamsCarrier *p) {
+  const std::string path = p->getString("inputBatchFile", "../geliosphere_batch_input_paramaters.csv");
+  const std::string home = cwd();
+  std::vector<Planned> plan;
+  if (!planBatch(p, path, true, plan)) return;
   if (plan.empty()) return;
   gelio_ctx *ctx = ghost::context();
   if (!ctx) return;

@@ -35,6 +35,8 @@ def load():
         "gelio_host_put_string": (None, [c_char_p, c_char_p]),
         "gelio_host_load_settings": (c_int32, [c_char_p]),
         "gelio_host_resolve": (c_int32, [c_int32, POINTER(abi.SimParams)]),
+        "gelio_host_batch_plan": (c_int32, [c_char_p, POINTER(abi.SimParams), POINTER(c_int32), c_int32,
+                                            POINTER(c_int32)]),
         "gelio_host_write_spectra": (c_int32, [c_int32, POINTER(abi.Spectra), c_int32, c_char_p]),
         "gelio_host_log_line": (c_int32, [c_int32, POINTER(abi.ExitRecord), c_float, c_char_p, c_int32]),
         "gelio_host_carrington_rotation": (c_int32, [c_int32, c_int32]),
@@ -64,3 +66,15 @@ def get_string(key: str, default: str = "") -> str:
     buf = ctypes.create_string_buffer(4096)
     load().gelio_host_get_string(key.encode(), default.encode(), buf, 4096)
     return buf.value.decode()
+
+
+def batch_plan(csv_path: str, cap: int = 256):
+    """(gelio_sim_params, 1-based CSV row) of every batch row that would run,
+    resolved in the current directory as batch mode resolves it."""
+    out = (abi.SimParams * cap)()
+    rows = (c_int32 * cap)()
+    n = c_int32()
+    st = load().gelio_host_batch_plan(csv_path.encode(), out, rows, cap, ctypes.byref(n))
+    if st != 0:
+        raise ValueError(f"gelio_host_batch_plan: status {st}")
+    return [(out[i], rows[i]) for i in range(min(n.value, cap))]

@@ -6,6 +6,7 @@
 #include <cstring>
 #include <string>
 #include <unistd.h>
+#include <vector>
 
 #include "Algorithms.hpp"
 #include "Engine.hpp"
@@ -58,6 +59,21 @@ int32_t gelio_host_load_settings(const char *path) {
 int32_t gelio_host_resolve(int32_t model, gelio_sim_params *out) {
   if (!out || model < 0 || model > GELIO_MODEL_2D_GELIOSPHERE) return GELIO_ERR_INVALID_ARGUMENT;
   *out = ghost::resolveSimParams(ParamsCarrier::instance(), model);
+  return GELIO_OK;
+}
+
+int32_t gelio_host_batch_plan(const char *csv_path, gelio_sim_params *out, int32_t *rows, int32_t cap,
+                              int32_t *n) {
+  if (!csv_path || !n || cap < 0) return GELIO_ERR_INVALID_ARGUMENT;
+  std::vector<gelio_sim_params> sims;
+  std::vector<int> rr;
+  const int k = batchPlan(ParamsCarrier::instance(), csv_path, sims, rr);
+  if (k < 0) return GELIO_ERR_INVALID_ARGUMENT;
+  for (int i = 0; i < k && i < cap; ++i) {
+    if (out) out[i] = sims[(size_t)i];
+    if (rows) rows[i] = rr[(size_t)i];
+  }
+  *n = k;
   return GELIO_OK;
 }
 

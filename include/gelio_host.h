@@ -53,6 +53,17 @@ int32_t gelio_host_load_settings(const char *path);
  * (CUDAKernel/src/CosmicConstants.cu:43-111). */
 int32_t gelio_host_resolve(int32_t model, gelio_sim_params *out);
 
+/* Resolve the rows of a batch CSV as batch mode does, without running them:
+ * each row that would run gets its results directory and simulation_log.txt
+ * (relative to the current directory) and its gelio_sim_params in out[k]
+ * with its 1-based CSV row in rows[k] (either may be NULL); at most cap are
+ * copied and *n receives how many rows resolve.  GELIO_OK, or
+ * GELIO_ERR_INVALID_ARGUMENT when the file cannot be read or its names are
+ * not unique (replaces the planning half of BatchRun::runAlgorithm,
+ * Algorithm/src/BatchRun.cpp:26-100). */
+int32_t gelio_host_batch_plan(const char *csv_path, gelio_sim_params *out, int32_t *rows, int32_t cap,
+                              int32_t *n);
+
 /* Write one model's spectrum files (the evaluators' names and formats) for
  * `s` into directory `dir` (NULL = current); 0 on success
  * (replaces the writeSpectrum calls of Algorithm/src/TwoDimensionBpResults.cpp:103-133,

@@ -193,3 +193,77 @@ def test_month_year_lookup_2d(fresh, tmp_path):
     assert fresh.gelio_host_get_float(b"K0", 0) == np.float32(2.5e-5)
     assert fresh.gelio_host_get_float(b"tilt_angle", 0) == np.float32(73.9)
     assert fresh.gelio_host_get_int(b"polarity", 0) == -1
+
+
+BATCH_HEADER = "name,month,year,V,K0,dt,r,theta,N,model,pathToCustomSettingsFile\n"
+
+
+def test_batch_plan_reference_row_quirks(fresh, tmp_path, monkeypatch):
+    """Batch rows resolve as Algorithm/src/BatchRun.cpp:26-79 and
+    BatchRun.cpp:282-342 do: a row with an unsupported model is skipped
+    without erasing the map, so its dt and N (put with insert semantics)
+    outlive it and win over the next row's own; a V out of range returns true
+    before the row's name and settings are applied; month without year,
+    'batch run' and dt out of range skip the row."""
+    monkeypatch.chdir(tmp_path)
+    monkeypatch.setenv("GELIO_SEED", "7")
+    settings = tmp_path / "custom.toml"
+    settings.write_text("[default_values]\nK0 = 5e22\nV = 400.0\ndt = 20.0\nr_injection = 1.0\n"
+                        "uniform_energy_injection_maximum = 101.0\n[2d_models_common_settings]\n"
+                        "theta_injection = 90.0\nuse_uniform_injection = false\n[SolarProp_like_model_settings]\n"
+                        "SolarProp_ratio = 0.02\n[Geliosphere_model_settings]\nGeliosphere_ratio = 0.2\n"
+                        "K0_ratio = 1.0\nC_delta = 8.7e-5\ndefault_tilt_angle = 0.1\n[advanced_settings]\n"
+                        "remove_log_files_after_simulation = true\n")
+    rows = ["a,,,,,,,,1,2D Geliosphere,",              # 1: runs, batch default settings (dt 50)
+            "b,,,,,100,,,1,3D Nope,",                  # 2: unsupported model, dt 100 stays in the map
+            "c,,,,,200,,,2,1D Fp,",                    # 3: runs at the leaked dt 100 and N 1
+            "d,5,,,,,,,1,1D Bp,",                      # 4: month without year
+            "e,,,,,,,,1,batch run,",                   # 5: batch run as a model
+            "f,,,50,,,,,1,2D Geliosphere,",            # 6: V out of range: defaults, generated name
+            "g,,,,,2,,,1,1D Fp,",                      # 7: dt out of range
+            f"h,,,,,,3.5,,1,2D SolarProp-like,{settings}"]  # 8: custom settings, r from the row
+    csv = tmp_path / "batch.csv"
+    csv.write_text(BATCH_HEADER + "\n".join(rows) + "\n")
+    plan = host.batch_plan(str(csv))
+    assert [r for _, r in plan] == [1, 3, 6, 8]
+    s1, s3, s6, s8 = (s for s, _ in plan)
+    assert (s1.model, s1.dt) == (abi.GELIO_MODEL_2D_GELIOSPHERE, 50.0)
+    assert (s3.model, s3.dt) == (abi.GELIO_MODEL_1D_FP, 100.0)
+    # N is put with insert semantics too: row 2's one million outlives it
+    assert s3.n_particles == -(-1_000_000 // 4096) * 4096
+    # row 6 runs on the kernels' constant defaults: no settings were loaded
+    assert (s6.model, s6.dt) == (abi.GELIO_MODEL_2D_GELIOSPHERE, 5.0)
+    assert np.float32(s6.K0) == np.float32(0.000222) and np.float32(s6.V) == np.float32(2.66667e-6)
+    assert (s8.model, s8.dt) == (abi.GELIO_MODEL_2D_SOLARPROP, 20.0)
+    assert np.float32(s8.r_injection) == np.float32(3.5)
+    assert s8.injection == abi.GELIO_INJ_SOLARPROP_GRID
+    # per-row seeds: the process seed plus the row's odd multiple
+    golden = 0x9E3779B97F4A7C15
+    assert [s.seed for s, _ in plan] == [(7 + r * golden) % (1 << 64) for r in (1, 3, 6, 8)]
+    res = tmp_path / "results"
+    assert (res / "Geliosphere2D" / "a" / "simulation_log.txt").exists()
+    assert (res / "1DFP" / "c" / "simulation_log.txt").exists()
+    assert (res / "SOLARPROPLike" / "h" / "simulation_log.txt").exists()
+    gen = [d.name for d in (res / "Geliosphere2D").iterdir() if d.name != "a"]
+    assert len(gen) == 1 and "_dt=" in gen[0] and (res / "Geliosphere2D" / gen[0] / "simulation_log.txt").exists()
+    for skipped in ("b", "d", "e", "f", "g"):
+        assert not any((res / m / skipped).exists() for m in ("Geliosphere2D", "1DFP", "1DBP", "SOLARPROPLike"))
+    assert "Model: 1D Fp" in (res / "1DFP" / "c" / "simulation_log.txt").read_text()
+    assert os.getcwd() == str(tmp_path)
+
+
+def test_batch_plan_rejects_duplicate_names_and_missing_file(fresh, tmp_path, monkeypatch):
+    monkeypatch.chdir(tmp_path)
+    csv = tmp_path / "dup.csv"
+    csv.write_text(BATCH_HEADER + "x,,,,,,,,1,1D Fp,\n y ,,,,,,,,1,1D Bp,\nx,,,,,,,,1,1D Bp,\n")
+    with pytest.raises(ValueError):
+        host.batch_plan(str(csv))
+    with pytest.raises(ValueError):
+        host.batch_plan(str(tmp_path / "absent.csv"))
+    assert not (tmp_path / "results").exists()
+    # blank names do not collide; generated names of rows resolved in the
+    # same second with equal dt/K0/V are kept apart
+    csv.write_text(BATCH_HEADER + ",,,,,,,,1,1D Fp,\n,,,,,,,,1,1D Fp,\n")
+    plan = host.batch_plan(str(csv))
+    assert [r for _, r in plan] == [1, 2]
+    assert len(list((tmp_path / "results" / "1DFP").iterdir())) == 2

@@ -393,6 +393,18 @@ __device__ __forceinline__ void draw(const Lane<R> &L, R *z) {
   }
 }
 
+// The 1D models draw the normals of their next group of four steps while the
+// current group integrates: the Philox rounds and Box-Muller do not depend
+// on the trajectory, so they fill the latency of the step's dependent chain.
+template <int MODEL> struct Prefetch {
+  static constexpr bool value = (MODEL == kModelFp || MODEL == kModelBp);
+};
+
+template <int MODEL, class R>
+__device__ __forceinline__ void draw_group(const Lane<R> &L, uint32_t group, R *z) {
+  normals4<R>(L.key0, L.key1, group, kStreamSde, L.pid, z);
+}
+
 __device__ __forceinline__ int find_group_index(const unsigned long long *prefix, int n,
                                                 unsigned long long t, int hint) {
   if (hint >= 0 && hint < n && prefix[hint] <= t && t < prefix[hint + 1]) return hint;
@@ -437,8 +449,12 @@ __global__ void __launch_bounds__(256, MINB) k_persistent(const KArgs a) {
   Consts<R> K;
   SimDev sd;
   bool active = false, drained = false;
+  // warp-uniform: every ticket is handed out, so no lane of this warp will
+  // be refilled again and the window grows to cut the per-window votes
+  bool exhausted = false;
   int slot = 0, g = -1;
   unsigned window = 0;
+  R zq[4] = {R(0), R(0), R(0), R(0)};     // 1D models: normals of the lane's next step group
 
   for (;;) {
     // 1) evaluate and bin queued exits, 32 at a time with every lane busy
@@ -477,6 +493,7 @@ __global__ void __launch_bounds__(256, MINB) k_persistent(const KArgs a) {
       unsigned long long base = 0;
       if (lane == leader) base = atomicAdd(&a.ctl->ticket[MODEL], (unsigned long long)__popc(need));
       base = __shfl_sync(kFull, base, leader);
+      if (base + (unsigned long long)__popc(need) >= total) exhausted = true;
       if (!active && !drained) {
         const unsigned long long t = base + __popc(need & lanemask_lt());
         if (t < total) {
@@ -485,6 +502,7 @@ __global__ void __launch_bounds__(256, MINB) k_persistent(const KArgs a) {
           sd = a.sims[sim];
           slot = g;
           init_lane<MODEL, R>(L, K, sd, a.inj_tables + (size_t)sim * GELIO_GRID_MAX, sim, t - gpre[g]);
+          if constexpr (Prefetch<MODEL>::value) draw_group<MODEL, R>(L, 0u, zq);
           sink.add(slot, sim, kOffNParticles, 1.0);
           active = true;
         } else {
@@ -499,12 +517,19 @@ __global__ void __launch_bounds__(256, MINB) k_persistent(const KArgs a) {
       }
       break;
     }
-    // 3) integrate `refill` steps
+    // 3) integrate `refill` steps (at least 64 once the tickets are exhausted)
     constexpr int spc = StepsPerCall<MODEL>::value;
-    for (int k = 0; k < a.refill; k += spc) {
+    const int win = (exhausted && a.refill < 64) ? 64 : a.refill;
+    for (int k = 0; k < win; k += spc) {
       if (active) {
         R z[4];
-        draw<MODEL, R>(L, z);
+        if constexpr (Prefetch<MODEL>::value) {
+#pragma unroll
+          for (int j = 0; j < 4; ++j) z[j] = zq[j];
+          draw_group<MODEL, R>(L, L.steps / spc + 1u, zq);
+        } else {
+          draw<MODEL, R>(L, z);
+        }
 #pragma unroll
         for (int j = 0; j < spc; ++j) {
           if (active) {

@@ -207,8 +207,7 @@ __device__ __forceinline__ void append_record_one(const KArgs &a, const Lane<R> 
 // Warp-aggregated flush of the pending exits of the lanes in `mask` (all of
 // which execute this call).  Backward models only.
 template <int MODEL>
-__device__ __noinline__ void flush_pending(const KArgs &a, const Sink<MODEL> &sink,
-                                              unsigned mask, const Pending &p) {
+__device__ __noinline__ void flush_pending(const Sink<MODEL> &sink, unsigned mask, const Pending &p) {
   constexpr int NV = 13;   // w[3], w2[3], gw[3], gw2[3], count
   const int lane = threadIdx.x & 31;
   Contribution C;
@@ -322,49 +321,74 @@ __device__ __forceinline__ void flush_queue(const KArgs &a, const Sink<MODEL> &s
     p.sim = e.sim;
     p.slot = (int)(e.slot_gbin & 0xffffu);
     p.gbin = (int)(e.slot_gbin >> 16) - 1;
-    flush_pending<MODEL>(a, sink, mask, p);
+    flush_pending<MODEL>(sink, mask, p);
   }
 }
 
-// Direct (non-aggregated) F-p record at a 1 AU crossing.
+// Direct (non-aggregated) F-p record of one 1 AU crossing, passed by value:
+// a reference to the lane, the simulation or the kernel arguments would put
+// them in local memory for the whole step loop (the call is out of line),
+// lengthening every step.
+struct FpCrossing {
+  float Tinj, Texit, rrec, sumac;
+  int sim, slot, grid_bins;
+  unsigned long long pid;
+  double grid_log_lo, grid_inv_dlog;
+};
+
 template <class R>
-__device__ __noinline__ void emit_fp(const KArgs &a, const Sink<kModelFp> &sink, int slot,
-                                        const SimDev &sd, const Lane<R> &L) {
-  const float Texit = (float)L.T.v;
-  const double p100 = round6(p_si((double)L.Tinj));
-  const double p1 = round6(p_si((double)Texit));
-  const double rr = round6((double)L.rrec);
-  const double sm = round6((double)(float)L.sumac.v);
+__device__ __forceinline__ FpCrossing fp_crossing(const Lane<R> &L, const SimDev &sd, int slot) {
+  FpCrossing x;
+  x.Tinj = L.Tinj;
+  x.Texit = (float)L.T.v;
+  x.rrec = L.rrec;
+  x.sumac = (float)L.sumac.v;
+  x.sim = L.sim;
+  x.slot = slot;
+  x.grid_bins = sd.grid_bins;
+  x.pid = L.pid;
+  x.grid_log_lo = sd.grid_log_lo;
+  x.grid_inv_dlog = sd.grid_inv_dlog;
+  return x;
+}
+
+static __device__ __noinline__ void emit_fp(Control *ctl, gelio_exit_record *records,
+                                     unsigned long long record_capacity, Sink<kModelFp> sink,
+                                     FpCrossing x) {
+  const double p100 = round6(p_si((double)x.Tinj));
+  const double p1 = round6(p_si((double)x.Texit));
+  const double rr = round6((double)x.rrec);
+  const double sm = round6((double)x.sumac);
   Contribution C;
   double T1;
   eval_fp(p100, p1, rr, sm, c_tables, C, T1);
-  const int s = L.sim;
+  const int s = x.sim, slot = x.slot;
   const double w = C.w[0], w2 = w * w;
   if (C.b_log >= 0) { sink.add(slot, s, kOffLogW + C.b_log, w); sink.add(slot, s, kOffLogW2 + C.b_log, w2); sink.add(slot, s, kOffLogN + C.b_log, 1.0); }
   if (C.b_e2) { sink.add(slot, s, kOffE2W + C.b_e2 - 1, w); sink.add(slot, s, kOffE2W2 + C.b_e2 - 1, w2); sink.add(slot, s, kOffE2N + C.b_e2 - 1, 1.0); }
   if (C.b_e3) { sink.add(slot, s, kOffE3W + C.b_e3 - 1, w); sink.add(slot, s, kOffE3W2 + C.b_e3 - 1, w2); sink.add(slot, s, kOffE3N + C.b_e3 - 1, 1.0); }
   if (C.b_e4) { sink.add(slot, s, kOffE4W + C.b_e4 - 1, w); sink.add(slot, s, kOffE4W2 + C.b_e4 - 1, w2); sink.add(slot, s, kOffE4N + C.b_e4 - 1, 1.0); }
-  const int gb = grid_log_bin(T1, sd.grid_log_lo, sd.grid_inv_dlog, sd.grid_bins);
+  const int gb = grid_log_bin(T1, x.grid_log_lo, x.grid_inv_dlog, x.grid_bins);
   if (gb >= 0) {
     sink.add(slot, s, kOffGridW + gb, w);
     sink.add(slot, s, kOffGridW2 + gb, w2);
     sink.add(slot, s, kOffGridN + gb, 1.0);
   }
   sink.add(slot, s, kOffNRecords, 1.0);
-  if (a.records != nullptr) {
-    const unsigned long long idx = atomicAdd(&a.ctl->rec_count, 1ull);
-    if (idx < a.record_capacity) {
+  if (records != nullptr) {
+    const unsigned long long idx = atomicAdd(&ctl->rec_count, 1ull);
+    if (idx < record_capacity) {
       gelio_exit_record rec;
-      rec.particle = (int64_t)L.pid;
-      rec.sim = L.sim;
-      rec.t_injection = L.Tinj;
-      rec.t_exit = Texit;
-      rec.r = L.rrec;
+      rec.particle = (int64_t)x.pid;
+      rec.sim = s;
+      rec.t_injection = x.Tinj;
+      rec.t_exit = x.Texit;
+      rec.r = x.rrec;
       rec.theta = 0.0f;
-      rec.sumac = (float)L.sumac.v;
-      a.records[idx] = rec;
+      rec.sumac = x.sumac;
+      records[idx] = rec;
     } else {
-      atomicAdd(&a.ctl->rec_dropped, 1ull);
+      atomicAdd(&ctl->rec_dropped, 1ull);
     }
   }
 }
@@ -537,7 +561,8 @@ __global__ void __launch_bounds__(256, MINB) k_persistent(const KArgs a) {
             ++L.steps;
             if (res != kContinue) {
               if constexpr (MODEL == kModelFp) {
-                if (res == kRecordAndContinue || res == kRecordAndStop) emit_fp<R>(a, sink, slot, sd, L);
+                if (res == kRecordAndContinue || res == kRecordAndStop)
+                  emit_fp(a.ctl, a.records, a.record_capacity, sink, fp_crossing(L, sd, slot));
                 if (res != kRecordAndContinue) {
                   active = false;
                   sink.add(slot, L.sim, kOffNSteps, (double)L.steps);
@@ -623,7 +648,8 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4) ? 2 : 1) k_plain(const K
           ++nrec;
         }
         if constexpr (MODEL == kModelFp) {
-          if (res == kRecordAndContinue || res == kRecordAndStop) emit_fp<R>(a, sink, 1 << 30, sd, L);
+          if (res == kRecordAndContinue || res == kRecordAndStop)
+            emit_fp(a.ctl, a.records, a.record_capacity, sink, fp_crossing(L, sd, 1 << 30));
           if (res != kContinue && res != kRecordAndContinue) { active = false; status = (nrec > 0) ? 0 : 1; }
         } else if (res != kContinue) {
           active = false;
@@ -650,7 +676,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 4) ? 2 : 1) k_plain(const K
     const unsigned pm = __ballot_sync(kFull, pending);
     if (pending) {
       append_records(a, pm, pd, MODEL);
-      flush_pending<MODEL>(a, sink, pm, pd);
+      flush_pending<MODEL>(sink, pm, pd);
     }
   }
   if (valid && a.replay != nullptr) {

@@ -610,11 +610,18 @@ def main():
         # the same workload with FP64 steps (B-p: the FP64-step variant)
         fp64 = None
         if args.workload == "bp":
-            eng.run(sims, precision=abi.GELIO_PREC_FP64)
+            # FP64 steps run ~50x slower on this part: time a bounded sample
+            # (the first 10^6 particles of the same simulation, every grid
+            # point equally represented) after a small warm-up run
+            import copy
+            warm, sample = copy.copy(sims[0]), copy.copy(sims[0])
+            warm.n_particles = 4096
+            sample.n_particles = min(sims[0].n_particles, 1_000_000)
+            eng.run([warm], precision=abi.GELIO_PREC_FP64)
             t0 = time.perf_counter()
-            r64 = eng.run(sims, precision=abi.GELIO_PREC_FP64)
-            fp64 = {"value": total_traj / (time.perf_counter() - t0), "unit": "trajectories/s",
-                    "kernel_ms": r64.stats.kernel_ms}
+            r64 = eng.run([sample], precision=abi.GELIO_PREC_FP64)
+            fp64 = {"value": sample.n_particles / (time.perf_counter() - t0), "unit": "trajectories/s",
+                    "kernel_ms": r64.stats.kernel_ms, "sample": "%d particles" % sample.n_particles}
         line = {"metric": metric, "value": value, "unit": "trajectories/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_rank / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",

@@ -244,8 +244,76 @@ def cpu_baseline_sample(threads: int):
     return secs, ntraj, nrec, nsteps
 
 
+# bounded CPU samples of the 1D workloads: (chunks, contiguous particles per
+# chunk); chunks sit at evenly spaced offsets of the simulation, and 100
+# contiguous particles cover every point of the 100-point B-p grid
+PORT_SAMPLE_1D = {"bp": (32, 100), "fp": (100, 2000)}
+
+
+def cpu_port_sample_1d(sim, workload: str, threads: int):
+    """The FP64 oracle port of the per-particle path (same Philox streams,
+    same injection) replaying a bounded sample of the workload's particles on
+    `threads` host threads; returns (seconds, trajectories, steps)."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import ffi
+    chunks, per = PORT_SAMPLE_1D[workload]
+    stride = max(per, int(sim.n_particles) // chunks)
+    offsets = [k * stride for k in range(chunks) if k * stride + per <= sim.n_particles]
+
+    def one(off):
+        _, steps, _, _ = ffi.replay(sim, off, per)
+        return int(steps.sum())
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        steps = sum(ex.map(one, offsets))
+    return time.perf_counter() - t0, len(offsets) * per, steps
+
+
+def port_sample_text(workload: str, threads: int, ntraj: int, secs: float) -> str:
+    chunks, per = PORT_SAMPLE_1D[workload]
+    return ("%d trajectories of the same workload (%d chunks of %d consecutive particles at evenly spaced "
+            "offsets) replayed by the FP64 oracle port on %d host threads, %.2f s"
+            % (ntraj, chunks, per, threads, secs))
+
+
+def run_reference_1d(args, world):
+    """Reference arm of the 1D workloads: the oracle's FP64 port of the
+    per-particle algorithm on a bounded sample of the same simulation."""
+    from geliosphere_gb300 import abi
+    from oracle import ffi
+    ffi.build()
+    threads = os.cpu_count() or 1
+    model = abi.GELIO_MODEL_1D_BP if args.workload == "bp" else abi.GELIO_MODEL_1D_FP
+    n = args.particles or (1_000_000 if args.workload == "fp" else 10_000_000)
+    sim = workload_1d(model, n, 0)[0]
+    for _ in range(args.warmup):
+        cpu_port_sample_1d(sim, args.workload, threads)
+    tot_s, tot_traj = 0.0, 0
+    for _ in range(args.steps):
+        secs, ntraj, _ = cpu_port_sample_1d(sim, args.workload, threads)
+        tot_s += secs
+        tot_traj += ntraj
+    v = tot_traj / tot_s
+    metric = ("1D B-p" if args.workload == "bp" else "1D F-p") + " trajectories/s"
+    sample = port_sample_text(args.workload, threads, tot_traj // args.steps, tot_s / args.steps)
+    line = {
+        "metric": metric, "value": v, "unit": "trajectories/s", "impl": "reference",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_s / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": " ".join(workload_1d.__doc__.split(";")[0 if args.workload == "bp" else 1].split()),
+                   "model": metric[:6], "particles": n, "sample": sample},
+        "cpu_baseline": {"value": v, "unit": "trajectories/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "trajectories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, rank, world):
     if rank != 0:
+        return
+    if args.workload in ("bp", "fp"):
+        run_reference_1d(args, world)
         return
     from oracle import ffi
     ffi.build()
@@ -531,7 +599,7 @@ def main():
     else:
         model = abi.GELIO_MODEL_1D_BP if args.workload == "bp" else abi.GELIO_MODEL_1D_FP
         metric = ("1D B-p" if args.workload == "bp" else "1D F-p") + " trajectories/s"
-        config = {"workload": workload_1d.__doc__.split(";")[0 if args.workload == "bp" else 1].strip(),
+        config = {"workload": " ".join(workload_1d.__doc__.split(";")[0 if args.workload == "bp" else 1].split()),
                   "model": metric[:6], "particles": args.particles,
                   "l2": "flushed between timed steps (256 MiB write)"}
         make = lambda n: workload_1d(model, n, rank)  # noqa: E731
@@ -632,6 +700,13 @@ def main():
                         "h2d_bytes_per_step": n * ctypes.sizeof(abi.SimParams),
                         "d2h_bytes_per_step": n * ctypes.sizeof(abi.Spectra)},
                 "gpu_launches": 6 * args.steps, "fp64_steps": fp64, "clocks": clk.summary()}
+        if not args.no_cpu_baseline and world == 1:
+            from oracle import ffi
+            ffi.build()
+            threads = os.cpu_count() or 1
+            secs, ntraj, _ = cpu_port_sample_1d(sims[0], args.workload, threads)
+            line["cpu_baseline"] = {"value": ntraj / secs, "unit": "trajectories/s", "cores": threads,
+                                    "kind": "port", "sample": port_sample_text(args.workload, threads, ntraj, secs)}
         print(json.dumps(line), flush=True)
         eng.close()
         return

@@ -473,8 +473,8 @@ __global__ void __launch_bounds__(256, MINB) k_persistent(const KArgs a) {
   Consts<R> K;
   SimDev sd;
   bool active = false, drained = false;
-  // warp-uniform: every ticket is handed out, so no lane of this warp will
-  // be refilled again and the window grows to cut the per-window votes
+  // 1D models, warp-uniform: every ticket is handed out, so no lane of this
+  // warp will be refilled again and the window grows to cut the votes
   bool exhausted = false;
   int slot = 0, g = -1;
   unsigned window = 0;
@@ -517,7 +517,7 @@ __global__ void __launch_bounds__(256, MINB) k_persistent(const KArgs a) {
       unsigned long long base = 0;
       if (lane == leader) base = atomicAdd(&a.ctl->ticket[MODEL], (unsigned long long)__popc(need));
       base = __shfl_sync(kFull, base, leader);
-      if (base + (unsigned long long)__popc(need) >= total) exhausted = true;
+      if (Prefetch<MODEL>::value && base + (unsigned long long)__popc(need) >= total) exhausted = true;
       if (!active && !drained) {
         const unsigned long long t = base + __popc(need & lanemask_lt());
         if (t < total) {
@@ -541,9 +541,9 @@ __global__ void __launch_bounds__(256, MINB) k_persistent(const KArgs a) {
       }
       break;
     }
-    // 3) integrate `refill` steps (at least 64 once the tickets are exhausted)
+    // 3) integrate `refill` steps (1D: at least 64 once the tickets are exhausted)
     constexpr int spc = StepsPerCall<MODEL>::value;
-    const int win = (exhausted && a.refill < 64) ? 64 : a.refill;
+    const int win = (Prefetch<MODEL>::value && exhausted && a.refill < 64) ? 64 : a.refill;
     for (int k = 0; k < win; k += spc) {
       if (active) {
         R z[4];

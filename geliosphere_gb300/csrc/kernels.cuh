@@ -146,6 +146,8 @@ __device__ __forceinline__ void init_lane(Lane<R> &L, Consts<R> &K, const SimDev
   } else {
     L.r.set((R)100.0001f);
     L.P.set(Math<R>::sqrt((R)Tinj * ((R)Tinj + R(2) * T0)));
+    L.Pt = L.P.v;
+    L.q = Math<R>::rsqrt(L.Pt * L.Pt + T0 * T0);
     L.sumac.set(R(0));
   }
   if (sd.grid_is_points) L.gbin = (int)(pid % (unsigned long long)sd.inj_points);

@@ -54,6 +54,7 @@ template <class R> struct Math;
 template <> struct Math<float> {
   static constexpr bool kCompensate = true;
   __device__ static __forceinline__ float sqrt(float x) { return sqrtf(x); }
+  __device__ static __forceinline__ float rsqrt(float x) { return rsqrtf(x); }
   __device__ static __forceinline__ float rcp(float x) { return __fdividef(1.0f, x); }
   __device__ static __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
   __device__ static __forceinline__ void sincos(float x, float *s, float *c) { sincosf(x, s, c); }
@@ -66,6 +67,7 @@ template <> struct Math<float> {
 template <> struct Math<double> {
   static constexpr bool kCompensate = false;
   __device__ static __forceinline__ double sqrt(double x) { return ::sqrt(x); }
+  __device__ static __forceinline__ double rsqrt(double x) { return ::rsqrt(x); }
   __device__ static __forceinline__ double rcp(double x) { return 1.0 / x; }
   __device__ static __forceinline__ double div(double a, double b) { return a / b; }
   __device__ static __forceinline__ void sincos(double x, double *s, double *c) { ::sincos(x, s, c); }
@@ -117,6 +119,7 @@ template <class R> struct Consts {
   R drift1;           // polarity * konvF * 1 / (3A)
   R dtheta_sp;        // SolarProp theta drift constant
   R adv;              // 1D: (2/3) V dt; 2D: (2/3) V dt as well
+  R sq2K0dt;          // sqrt(2 K0 dt)
 };
 
 template <class R>
@@ -142,6 +145,7 @@ __device__ __forceinline__ void make_consts(const SimDev &s, Consts<R> &k) {
   k.dtheta_sp = (s.flags & 1) ? -(R)s.polarity * (R)kKonvF * M::div(R(2), R(3) * (R)kA)
                               : (R)kDriftThetaConstantSP;
   k.adv = R(2) * V * k.dt * M::rcp(R(3));
+  k.sq2K0dt = M::sqrt(R(2) * k.K0 * k.dt);
 }
 
 // ---------------------------------------------------------------------------
@@ -176,6 +180,7 @@ __device__ __forceinline__ float inj_solarprop(unsigned long long s, const float
 // ---------------------------------------------------------------------------
 template <class R> struct Lane {
   Acc<R> r, th, T, P, sumac;
+  R Pt, q;             // F-p: the rigidity T was computed from, 1 / sqrt(Pt^2 + T0^2)
   float thn;           // FP32 2D models: theta = 2 pi thn + th once theta has left [0, 2 pi)
   float Tinj;
   float rrec;          // F-p: r of the last 1 AU crossing, before a reflection undoes the step
@@ -496,20 +501,32 @@ __device__ __forceinline__ int step_bp(Lane<R> &L, const Consts<R> &k, R z) {
 template <class R>
 __device__ __forceinline__ int step_fp(Lane<R> &L, const Consts<R> &k, R z) {
   using M = Math<R>;
-  const R r = L.r.v, T = L.T.v;
+  const R r = L.r.v;
   const R T0 = (R)kT0;
-  const R P0 = M::sqrt(T * (T + T0 + T0));
-  const R beta = P0 * M::rcp(T + T0);
+  // Rigidity and beta of the current T from the momentum Pt that T was
+  // computed from and q = 1 / sqrt(Pt^2 + T0^2) = 1 / (T + T0), both carried
+  // from the previous step: sqrt(T (T + 2 T0)) = Pt and Pt / (T + T0) = Pt q
+  // in exact arithmetic.  This takes two square roots and a reciprocal off
+  // the step's dependent chain; an F-p run is bounded by the latency of its
+  // longest trajectory.
+  const R Pt = L.Pt, q = L.q;
+  const R beta = Pt * q;
   const R inv_r = M::rcp(r);
   L.sumac.add(R(2) * k.adv * inv_r);                    // Eq. 11: 4 V dt / (3 r)
   const Acc<R> Psave = L.P;
   const Acc<R> rsave = L.r;
   L.P.add(-k.adv * L.P.v * inv_r);                      // Eq. 10
-  const R Kdiff = k.K0 * beta * P0;                     // Eq. 7
-  const R dr = (k.V + R(2) * Kdiff * inv_r) * k.dt + z * M::sqrt(R(2) * Kdiff * k.dt);   // Eq. 9
+  const R Kdiff = k.K0 * beta * Pt;                     // Eq. 7
+  // Eq. 9; sqrt(2 Kdiff dt) = Pt sqrt(2 K0 dt) sqrt(q)
+  const R dr = (k.V + R(2) * Kdiff * inv_r) * k.dt + z * (Pt * k.sq2K0dt * M::sqrt(q));
   L.r.add(dr);
-  const R Tn = kinetic_from_rigidity(L.P.v);
+  const R Pn = L.P.v;
+  const R xn = Pn * Pn + T0 * T0;
+  const R qn = M::rsqrt(xn);
+  const R Tn = Pn * Pn * M::rcp(xn * qn + T0);          // P^2 / (sqrt(P^2 + T0^2) + T0)
   L.T.set(Tn);
+  L.Pt = Pn;                     // T keeps the rejected step's value if the step is undone below
+  L.q = qn;
   const R rn = L.r.v;
   int res = kContinue;
   if (beta > (R)0.01f && Tn < R(100)) {

@@ -431,6 +431,38 @@ __device__ __forceinline__ void draw_group(const Lane<R> &L, uint32_t group, R *
   normals4<R>(L.key0, L.key1, group, kStreamSde, L.pid, z);
 }
 
+// Particle handed out by the u-th ticket of a simulation of n particles.
+// On a grid injection (particle i takes grid point i mod P, the energies
+// ascending with the point) the tickets walk the points in ascending order:
+// the lowest energies, whose trajectories are the longest, start first and
+// the run does not end waiting for a long trajectory that started late.
+// Every particle is still handed out exactly once, and a trajectory depends
+// only on its index, so the results do not change.
+__device__ __forceinline__ unsigned long long ticket_particle(unsigned long long u, unsigned long long n,
+                                                              unsigned long long P) {
+  // (32-bit arithmetic; a simulation of 2^32 particles or more keeps index order)
+  if (P <= 1 || n <= P || n > 0xffffffffull) return u;
+  const uint32_t uu = (uint32_t)u, p = (uint32_t)P;
+  const uint32_t qv = (uint32_t)n / p, rm = (uint32_t)n % p;   // points g < rm hold qv + 1 particles
+  const uint32_t head = rm * (qv + 1u);
+  uint32_t g, k;
+  if (uu < head) {
+    g = uu / (qv + 1u);
+    k = uu - g * (qv + 1u);
+  } else {
+    const uint32_t v = uu - head;
+    g = rm + v / qv;
+    k = v - (g - rm) * qv;
+  }
+  return (unsigned long long)g + (unsigned long long)p * k;
+}
+
+__device__ __forceinline__ unsigned long long grid_points(const SimDev &sd) {
+  if (sd.injection == GELIO_INJ_LOG_GRID) return (unsigned long long)sd.inj_points;
+  if (sd.injection == GELIO_INJ_SOLARPROP_GRID) return 30ull;
+  return 0ull;
+}
+
 __device__ __forceinline__ int find_group_index(const unsigned long long *prefix, int n,
                                                 unsigned long long t, int hint) {
   if (hint >= 0 && hint < n && prefix[hint] <= t && t < prefix[hint + 1]) return hint;
@@ -527,7 +559,8 @@ __global__ void __launch_bounds__(256, MINB) k_persistent(const KArgs a) {
           const int sim = gsim[g];
           sd = a.sims[sim];
           slot = g;
-          init_lane<MODEL, R>(L, K, sd, a.inj_tables + (size_t)sim * GELIO_GRID_MAX, sim, t - gpre[g]);
+          const unsigned long long pid = ticket_particle(t - gpre[g], gpre[g + 1] - gpre[g], grid_points(sd));
+          init_lane<MODEL, R>(L, K, sd, a.inj_tables + (size_t)sim * GELIO_GRID_MAX, sim, pid);
           if constexpr (Prefetch<MODEL>::value) draw_group<MODEL, R>(L, 0u, zq);
           sink.add(slot, sim, kOffNParticles, 1.0);
           active = true;

@@ -18,16 +18,13 @@ struct Philox4 {
   uint32_t x, y, z, w;
 };
 
+// One widening multiply gives both halves (a single mul.wide.u32 instead of
+// a mul.lo and a mul.hi).
 __host__ __device__ __forceinline__ void philox_mulhilo(uint32_t a, uint32_t b,
                                                         uint32_t &hi, uint32_t &lo) {
-#if defined(__CUDA_ARCH__)
-  lo = a * b;
-  hi = __umulhi(a, b);
-#else
   const uint64_t p = (uint64_t)a * (uint64_t)b;
   lo = (uint32_t)p;
   hi = (uint32_t)(p >> 32);
-#endif
 }
 
 __host__ __device__ __forceinline__ Philox4 philox4x32_10(Philox4 c, uint32_t k0, uint32_t k1) {
@@ -52,9 +49,11 @@ __host__ __device__ __forceinline__ Philox4 philox4x32_10(Philox4 c, uint32_t k0
 
 // 23-bit uniform in (0, 1): (x >> 9) * 2^-23 + 2^-24 = (2 (x >> 9) + 1) 2^-24,
 // an odd multiple of 2^-24 below 1, so exactly representable in FP32 (and
-// identical in the FP64 oracle); never 0, so log() is finite.
+// identical in the FP64 oracle); never 0, so log() is finite.  Built from the
+// bits: 1 + m 2^-23 (exponent of 1, mantissa m) minus (1 - 2^-24); the
+// difference is exact (Sterbenz), so no conversion instruction is needed.
 __device__ __forceinline__ float u32_to_unit(uint32_t x) {
-  return __uint2float_rn(2u * (x >> 9) + 1u) * 5.9604644775390625e-8f;
+  return __uint_as_float(0x3f800000u | (x >> 9)) - 0.99999994f;
 }
 
 // Box-Muller: z0 = sqrt(-2 ln u1) cos(2 pi u2), z1 = sqrt(-2 ln u1) sin(2 pi u2).

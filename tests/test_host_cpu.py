@@ -267,3 +267,15 @@ def test_batch_plan_rejects_duplicate_names_and_missing_file(fresh, tmp_path, mo
     plan = host.batch_plan(str(csv))
     assert [r for _, r in plan] == [1, 2]
     assert len(list((tmp_path / "results" / "1DFP").iterdir())) == 2
+
+
+def test_batch_plan_cell_conversion(fresh, tmp_path, monkeypatch):
+    """Cells convert as rapidcsv's default converter does: empty or
+    non-numeric cells read as -1 (unset), numeric text in any float form."""
+    monkeypatch.chdir(tmp_path)
+    csv = tmp_path / "cells.csv"
+    csv.write_text(BATCH_HEADER + "a,,,,,abc,,,1,1D Bp,\nb,,,,,1e2,,,1,1D Bp,\nc,,,,,75.5,,,x,1D Bp,\n")
+    plan = host.batch_plan(str(csv))
+    assert [r for _, r in plan] == [1, 2, 3]
+    assert [s.dt for s, _ in plan] == [50.0, 100.0, 75.5]     # unset dt: the batch default settings' 50
+    assert plan[2][0].n_particles == -(-1_000_000 // 4096) * 4096   # N "x": unset, one million

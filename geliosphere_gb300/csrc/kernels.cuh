@@ -579,6 +579,7 @@ __global__ void __launch_bounds__(256, MINB) k_persistent(const KArgs a) {
     // 3) integrate `refill` steps (1D: at least 64 once the tickets are exhausted)
     constexpr int spc = StepsPerCall<MODEL>::value;
     const int win = (Prefetch<MODEL>::value && exhausted && a.refill < 64) ? 64 : a.refill;
+    const uint32_t cap32 = (a.max_steps > 0xffffffffull) ? 0xffffffffu : (uint32_t)a.max_steps;
     for (int k = 0; k < win; k += spc) {
       if (active) {
         R z[4];
@@ -589,20 +590,35 @@ __global__ void __launch_bounds__(256, MINB) k_persistent(const KArgs a) {
         } else {
           draw<MODEL, R>(L, z);
         }
+        if constexpr (MODEL == kModelFp) {
+          // F-p runs end on the latency of their longest chain: one test per
+          // step covers the rare events (a crossing record, a stop, the step
+          // cap), and a stopped lane leaves the group at once
 #pragma unroll
-        for (int j = 0; j < spc; ++j) {
-          if (active) {
-            const int res = model_step<MODEL, R>(L, K, z, j);
+          for (int j = 0; j < 4; ++j) {
+            const int res = step_fp(L, K, z[j]);
             ++L.steps;
-            if (res != kContinue) {
-              if constexpr (MODEL == kModelFp) {
-                if (res == kRecordAndContinue || res == kRecordAndStop)
-                  emit_fp(a.ctl, a.records, a.record_capacity, sink, fp_crossing(L, sd, slot));
-                if (res != kRecordAndContinue) {
-                  active = false;
-                  sink.add(slot, L.sim, kOffNSteps, (double)L.steps);
-                }
-              } else {
+            if (res != kContinue || L.steps >= cap32) {
+              if (res == kRecordAndContinue || res == kRecordAndStop)
+                emit_fp(a.ctl, a.records, a.record_capacity, sink, fp_crossing(L, sd, slot));
+              if (res == kRecordAndStop || res == kStop) {
+                active = false;
+                sink.add(slot, L.sim, kOffNSteps, (double)L.steps);
+              } else if (L.steps >= cap32) {
+                active = false;
+                sink.add(slot, L.sim, kOffNSteps, (double)L.steps);
+                sink.add(slot, L.sim, kOffNCapped, 1.0);
+              }
+              if (!active) break;
+            }
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < spc; ++j) {
+            if (active) {
+              const int res = model_step<MODEL, R>(L, K, z, j);
+              ++L.steps;
+              if (res != kContinue) {
                 active = false;
                 sink.add(slot, L.sim, kOffNSteps, (double)L.steps);
                 if (res == kRecordAndStop) {
@@ -618,11 +634,11 @@ __global__ void __launch_bounds__(256, MINB) k_persistent(const KArgs a) {
                   sink.add(slot, L.sim, kOffNLost, 1.0);
                 }
               }
-            }
-            if (active && L.steps >= a.max_steps) {
-              active = false;
-              sink.add(slot, L.sim, kOffNSteps, (double)L.steps);
-              sink.add(slot, L.sim, kOffNCapped, 1.0);
+              if (active && L.steps >= a.max_steps) {
+                active = false;
+                sink.add(slot, L.sim, kOffNSteps, (double)L.steps);
+                sink.add(slot, L.sim, kOffNCapped, 1.0);
+              }
             }
           }
         }

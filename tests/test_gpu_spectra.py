@@ -240,6 +240,24 @@ def test_1d_launch_variants_agree(engine, model, variant):
     _assert_same(a, b)
 
 
+@pytest.mark.parametrize("cap", [22, 64])
+def test_fp_step_cap_matches_plain_kernel(engine, cap):
+    """The F-p persistent loop tests the step cap together with the step's
+    rare events; a cap inside a group of four steps stops a trajectory at
+    the same step as the plain kernel's per-step test."""
+    n = 50_000
+    sim = make_sim(abi.GELIO_MODEL_1D_FP, n, dt=50, seed=5, injection=abi.GELIO_INJ_LOG_UNIFORM, inj_min=0.01,
+                   inj_max=1.0, grid_min=0.01, grid_max=200.0, grid_bins=60)
+    a = engine.run(sim, max_steps=cap)
+    b = engine.run(sim, max_steps=cap, plain=True)
+    assert a.status == abi.GELIO_WARN_STEP_CAP
+    assert a.stats.n_step_capped == b.stats.n_step_capped > 0
+    sa, sb = spectra_dict(a.spectra[0]), spectra_dict(b.spectra[0])
+    assert sa["n_steps"] == sb["n_steps"] <= cap * n
+    assert sa["n_records"] == sb["n_records"]
+    np.testing.assert_array_equal(sa["grid_n"], sb["grid_n"])
+
+
 def test_fp32_and_fp64_runs_agree(engine):
     sim = make_sim(abi.GELIO_MODEL_1D_BP, 20_000, dt=50, seed=8, injection=abi.GELIO_INJ_LOG_GRID,
                    inj_points=40, inj_min=0.05, inj_max=50.0)

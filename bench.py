@@ -17,8 +17,12 @@ e2e   : the same metric through gelio_run with host buffers (parameters
         sources are not available on this host).
 
 Other workloads (--workload; each prints its own line of the same form):
-  bp        1D B-p, 1e7 protons on a 100-point log grid, FP32 and FP64 steps
+  bp        1D B-p, 1e7 protons on a 100-point log grid, FP32 steps (FP64
+            steps on a 1e6-particle sample)
   fp        1D F-p, 1e6 protons log-uniform 0.01-200 GeV, 300 log bins
+            (bp and fp: cpu_baseline and --impl reference are the FP64
+            oracle port of the same per-particle path on a bounded sample of
+            the same simulation, on all host threads)
   batch256  256 random 2D simulations in one graph-captured persistent
             launch vs 256 plain launches (one per simulation)
   batch_cli the same kind of batch as a 256-row batch CSV through the

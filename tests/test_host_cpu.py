@@ -183,6 +183,13 @@ def test_month_year_lookup_1d(fresh, tmp_path):
     assert fresh.gelio_host_get_float(b"K0", 0) == np.float32(1.25e-4)
     assert fresh.gelio_host_get_float(b"V", 0) == np.float32(500.0 * 6.68458712e-9)
     assert fresh.gelio_host_get_int(b"month_option", 0) == 2
+    # the table's K0 is put without K0_entered_by_user, and setConstants
+    # applies a 1D model's K0 only when it is set (CosmicConstants.cu:68-72):
+    # a 1D month/year run keeps the default K0 and takes the table's V
+    sim = abi.SimParams()
+    assert fresh.gelio_host_resolve(abi.GELIO_MODEL_1D_BP, ctypes.byref(sim)) == 0
+    assert np.float32(sim.K0) == np.float32(0.000222)
+    assert np.float32(sim.V) == np.float32(np.float32(500.0 * 6.68458712e-9))
 
 
 def test_month_year_lookup_2d(fresh, tmp_path):
@@ -193,6 +200,11 @@ def test_month_year_lookup_2d(fresh, tmp_path):
     assert fresh.gelio_host_get_float(b"K0", 0) == np.float32(2.5e-5)
     assert fresh.gelio_host_get_float(b"tilt_angle", 0) == np.float32(73.9)
     assert fresh.gelio_host_get_int(b"polarity", 0) == -1
+    # 2D models do apply it (times K0_ratio, whose fallback is 5 without settings)
+    sim = abi.SimParams()
+    assert fresh.gelio_host_resolve(abi.GELIO_MODEL_2D_GELIOSPHERE, ctypes.byref(sim)) == 0
+    assert np.float32(sim.K0) == np.float32(np.float32(2.5e-5) * np.float32(5.0))
+    assert sim.polarity == -1.0
 
 
 BATCH_HEADER = "name,month,year,V,K0,dt,r,theta,N,model,pathToCustomSettingsFile\n"

@@ -291,3 +291,54 @@ def test_batch_plan_cell_conversion(fresh, tmp_path, monkeypatch):
     assert [r for _, r in plan] == [1, 2, 3]
     assert [s.dt for s, _ in plan] == [50.0, 100.0, 75.5]     # unset dt: the batch default settings' 50
     assert plan[2][0].n_particles == -(-1_000_000 // 4096) * 4096   # N "x": unset, one million
+
+
+def test_batch_plan_documented_input_shape(fresh, tmp_path, monkeypatch):
+    """A batch CSV of the shape the reference documents (its own column
+    order, month/year rows for the 2D model with r and theta, a row without a
+    name, a 1D row with K0 in 5E+022 form): each row resolves to the
+    simulation the reference would run, in its own directory.
+
+    Quirk kept: BatchRun::parseValues looks the date up before the row's
+    model is put into the map (Algorithm/src/BatchRun.cpp:58-64), and the map
+    was erased, so the lookup sees the default model "1D Fp": every batch
+    row, 2D included, reads K0 and V from the 1D table (K0_phi_table.csv)
+    and leaves tilt and polarity at their defaults."""
+    monkeypatch.chdir(tmp_path)
+    monkeypatch.setenv("GELIO_SEED", "11")
+    (tmp_path / "K0_phi_table.csv").write_text(
+        "year_week,moodulation_potentional,k0_au2/s,k0_m2/s,V,year,month\n"
+        "2000.04,700,2.5E-04,5.0E+018,450,2000,1\n"
+        "2000.12,710,2.0E-04,4.0E+018,520,2000,2\n")
+    (tmp_path / "Geliosphere_K0_phi_table.csv").write_text(    # not read in batch mode
+        "carrington_rotation,year_week,modulation_potentional,k0_au2/s,tilt_angle,year,month,day,polarity\n"
+        f"{fresh.gelio_host_carrington_rotation(1, 2000)},2000.01,752,9.9E-05,73.9,2000,1,1,-1\n")
+    fresh.gelio_host_put_string(b"currentApplicationPath", (str(tmp_path) + "/").encode())
+    csv = tmp_path / "batch.csv"
+    csv.write_text("year,month,K0,V,dt,N,r,theta,pathToCustomSettingsFile,name,model\n"
+                   "2000,1,,,100,2,1.25,80.5,,g1,2D Geliosphere\n"
+                   "2000,2,,,100,2,1.5,85,,g2,2D Geliosphere\n"
+                   "2000,1,,,100,1,2.0,90,,,2D Geliosphere\n"
+                   ",,5E+022,400,500,3,,,,Test,1D Fp\n")
+    plan = host.batch_plan(str(csv))
+    assert [r for _, r in plan] == [1, 2, 3, 4]
+    f32 = np.float32
+    deg = lambda x: f32(f32(f32(x) * f32(3.1415926535)) / f32(180.0))  # noqa: E731
+    for (sim, _), k0, v, r, th in zip(plan[:3], (2.5e-4, 2.0e-4, 2.5e-4), (450.0, 520.0, 450.0),
+                                      (1.25, 1.5, 2.0), (80.5, 85.0, 90.0)):
+        assert sim.model == abi.GELIO_MODEL_2D_GELIOSPHERE and sim.dt == 100.0
+        assert f32(sim.K0) == f32(f32(k0) * f32(1.0))        # batch default settings: K0_ratio 1
+        assert f32(sim.V) == f32(f32(v * 6.68458712e-9))
+        assert f32(sim.tilt) == deg(0.1) and sim.polarity == 1.0   # default tilt angle, polarity
+        assert f32(sim.r_injection) == f32(r) and f32(sim.theta_injection) == deg(th)
+    assert [s.n_particles for s, _ in plan] == [-(-m * 1_000_000 // 4096) * 4096 for m in (2, 2, 1, 3)]
+    fp = plan[3][0]
+    assert fp.model == abi.GELIO_MODEL_1D_FP and fp.dt == 500.0
+    assert f32(fp.K0) == f32(f32(5e22) * f32(4.4683705e-27))
+    assert f32(fp.V) == f32(f32(400.0) * f32(6.68458712e-9))
+    res = tmp_path / "results"
+    log = (res / "Geliosphere2D" / "g1" / "simulation_log.txt").read_text()
+    assert "Selected month: 1" in log and "Selected year: 2000" in log
+    assert (res / "Geliosphere2D" / "g2" / "simulation_log.txt").exists()
+    assert len([d for d in (res / "Geliosphere2D").iterdir() if d.name not in ("g1", "g2")]) == 1
+    assert "Model: 1D Fp" in (res / "1DFP" / "Test" / "simulation_log.txt").read_text()

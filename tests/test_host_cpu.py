@@ -338,7 +338,13 @@ def test_batch_plan_documented_input_shape(fresh, tmp_path, monkeypatch):
     assert f32(fp.V) == f32(f32(400.0) * f32(6.68458712e-9))
     res = tmp_path / "results"
     log = (res / "Geliosphere2D" / "g1" / "simulation_log.txt").read_text()
-    assert "Selected month: 1" in log and "Selected year: 2000" in log
+    tilt = f32(0.1)
+    expected = ["Model: 2D Geliosphere", "---------------------", "Selected month: 1", "Selected year: 2000",
+                "Geliosphere model ratio: %g" % f32(0.2), "C Delta: %g" % f32(8.7e-5),
+                "Loaded tilt angle from file: %g" % tilt,
+                "Calculated tilt angle:: %g" % f32(f32(tilt * f32(3.1415926535)) / f32(180.0)),
+                "dt: %g" % f32(100.0), "K0: %g" % f32(2.5e-4), "V: %g" % f32(450.0 * 6.68458712e-9)]
+    assert log.splitlines() == expected      # FileUtils.cpp:99-125 line for line
     assert (res / "Geliosphere2D" / "g2" / "simulation_log.txt").exists()
     assert len([d for d in (res / "Geliosphere2D").iterdir() if d.name not in ("g1", "g2")]) == 1
     assert "Model: 1D Fp" in (res / "1DFP" / "Test" / "simulation_log.txt").read_text()

@@ -299,6 +299,7 @@ void BatchRun::runAlgorithm(ParamsCarrier *p) {
   const int st = gelio_run(ctx, sims.data(), (int32_t)sims.size(), &opts, out.data(), &stats);
   if (st != GELIO_OK && st < GELIO_WARN_FIRST) {
     glog::error(std::string("Batch simulation failed: ") + gelio_status_string(st) + " " + gelio_last_error());
+    ghost::runFailed() = true;
     return;
   }
   if (st >= GELIO_WARN_FIRST) glog::warn(gelio_status_string(st));

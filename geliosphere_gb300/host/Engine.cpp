@@ -22,7 +22,13 @@ gelio_ctx *context() {
       ctx = nullptr;
     }
   }
+  if (!ctx) runFailed() = true;
   return ctx;
+}
+
+bool &runFailed() {
+  static bool failed = false;
+  return failed;
 }
 
 FusedSpectra &lastFused() {

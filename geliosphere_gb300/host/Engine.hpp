@@ -21,6 +21,11 @@ struct FusedSpectra {
 };
 FusedSpectra &lastFused();
 
+// Set when a simulation or an evaluation could not run on the GPU (no usable
+// device, an engine error): the executable then exits non-zero, as the
+// reference does when gpuErrchk ends the process (CudaErrorCheck.cuh:31-41).
+bool &runFailed();
+
 // gelio_sim_params for `model` from the parameter map, with the precedence
 // of setConstants / setSolarPropConstants / setGeliosphereModelConstants
 // (CUDAKernel/src/CosmicConstants.cu:43-111) and the __constant__ defaults

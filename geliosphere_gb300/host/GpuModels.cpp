@@ -39,6 +39,7 @@ bool runGpuModel(ParamsCarrier *p, int model) {
   const int st = gelio_run(ctx, &sim, 1, &opts, &fused.spectra, &stats);
   if (st != GELIO_OK && st < GELIO_WARN_FIRST) {
     glog::error(std::string("Simulation failed: ") + gelio_status_string(st) + " " + gelio_last_error());
+    ghost::runFailed() = true;
     return false;
   }
   if (st >= GELIO_WARN_FIRST) glog::warn(gelio_status_string(st));

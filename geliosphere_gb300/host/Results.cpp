@@ -74,6 +74,7 @@ static bool evaluateLog(ParamsCarrier *p, int model, gelio_spectra &out) {
   const int st = gelio_evaluate(ctx, model, rows.data(), n > 0 ? n : 0, ncol, &out);
   if (st != GELIO_OK) {
     glog::error(std::string("Evaluation failed: ") + gelio_status_string(st));
+    ghost::runFailed() = true;
     return false;
   }
   return true;

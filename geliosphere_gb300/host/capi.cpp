@@ -34,9 +34,10 @@ int32_t gelio_host_main(int32_t argc, char **argv) {
     glog::error("Selected custom model is not defined in factory.");
     return -1;
   }
+  ghost::runFailed() = false;
   a->runAlgorithm(p);
   delete a;
-  return 0;
+  return ghost::runFailed() ? 1 : 0;
 }
 
 int32_t gelio_host_parse(int32_t argc, char **argv) { return parseParams(argc, argv, ParamsCarrier::instance()); }

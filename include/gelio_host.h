@@ -21,8 +21,10 @@ extern "C" {
 #endif
 
 /* The application: parse argv, pick the algorithm by model name, run it.
- * Returns 0, or -1 when parsing fails or the model is unknown
- * (replaces main(), main.cpp:22-40). */
+ * Returns 0; -1 when parsing fails or the model is unknown; 1 when a
+ * simulation or evaluation could not run on the GPU (no usable device, an
+ * engine error), where the reference's gpuErrchk ends the process with the
+ * CUDA error code (replaces main(), main.cpp:22-40). */
 int32_t gelio_host_main(int32_t argc, char **argv);
 
 /* Parse argv into the process-wide parameter map; 1 on success

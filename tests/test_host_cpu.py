@@ -348,3 +348,31 @@ def test_batch_plan_documented_input_shape(fresh, tmp_path, monkeypatch):
     assert (res / "Geliosphere2D" / "g2" / "simulation_log.txt").exists()
     assert len([d for d in (res / "Geliosphere2D").iterdir() if d.name not in ("g1", "g2")]) == 1
     assert "Model: 1D Fp" in (res / "1DFP" / "Test" / "simulation_log.txt").read_text()
+
+
+def _exe_run(args, cwd):
+    import subprocess
+    if not os.path.exists(host.EXE):
+        host.build()
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES="")      # no device visible, on any machine
+    r = subprocess.run([host.EXE, *args], cwd=cwd, env=env, capture_output=True, text=True, timeout=120)
+    return r.returncode, r.stderr
+
+
+def test_exit_status_without_a_device(tmp_path):
+    """No CPU fallback: a run that cannot reach a GPU says so and exits
+    non-zero (the reference's gpuErrchk ends the process with the CUDA error
+    code); a parse error exits 255 (main returns -1); --cpu-only is reported
+    and exits 0 without touching the engine."""
+    rc, err = _exe_run(["-T", "-N", "1", "-p", "x"], tmp_path)
+    assert rc == 1 and "GPU engine unavailable" in err
+    # evaluation needs the engine too (a missing log.dat is only reported, as
+    # by the reference's evaluators)
+    rc, err = _exe_run(["-B", "--evaluation", os.path.join(GOLDEN, "eval_bp", "log.dat")], tmp_path)
+    assert rc == 1 and "GPU engine unavailable" in err
+    rc, err = _exe_run(["-B", "--evaluation", str(tmp_path / "missing.dat")], tmp_path)
+    assert rc == 0
+    rc, err = _exe_run(["-F", "-B"], tmp_path)
+    assert rc == 255
+    rc, err = _exe_run(["-T", "--cpu-only", "-N", "1", "-p", "c"], tmp_path)
+    assert rc == 0 and "CPU-only" in err

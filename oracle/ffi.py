@@ -23,10 +23,13 @@ class CpuParams(Structure):
     """Resolved statics of the reference CPU models (Constants.hpp:14-239)."""
     _fields_ = [(n, c_double) for n in
                 "V dt K0 ratio delta0 alphaM polarity rInit thetainj".split()] + [
-        ("useUniformInjection", c_int), ("uniformEnergyInjectionMaximum", c_double)]
+        ("useUniformInjection", c_int), ("uniformEnergyInjectionMaximum", c_double),
+        # not in the reference: an injection grid for the 2D block loop
+        # (null keeps the reference's injection)
+        ("inj_energies", POINTER(c_float)), ("inj_points", c_int), ("inj_per_point", c_int)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        return {k: getattr(self, k) for k, _ in self._fields_[:11]}
 
 
 def build(force: bool = False) -> str:
@@ -37,9 +40,17 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
-def build_reference(ref: str = "/root/reference") -> bool:
+def reference_dir() -> str:
+    """The reference sources: $GELIO_REFERENCE_DIR, else a `reference`
+    checkout beside this repository."""
+    return os.environ.get("GELIO_REFERENCE_DIR") or \
+        os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+
+
+def build_reference(ref: str | None = None) -> bool:
     """Compile the reference's own CPU models / evaluators (only where the
     reference sources exist)."""
+    ref = ref or reference_dir()
     if not os.path.isdir(ref):
         return False
     subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + ref], check=True)
@@ -68,6 +79,9 @@ def load():
     lib.gor_replay_f64.argtypes = [SP, c_int64, c_int64, c_uint64, POINTER(c_int32), POINTER(c_uint32),
                                    POINTER(c_int32), POINTER(c_double)]
     lib.gor_replay_f64.restype = c_int
+    lib.gor_replay_f64_noise.argtypes = [SP, c_int64, c_int64, c_uint64, c_double, c_int32, POINTER(c_int32),
+                                         POINTER(c_uint32), POINTER(c_int32), POINTER(c_double)]
+    lib.gor_replay_f64_noise.restype = c_int
     lib.gor_cpu_block.argtypes = [c_int, POINTER(CpuParams), c_int, c_int, c_int, c_uint32,
                                   POINTER(c_double), c_int64, POINTER(c_int64)]
     lib.gor_cpu_block.restype = c_int64
@@ -78,6 +92,9 @@ def load():
     lib.gor_cpu_baseline.argtypes = [c_int, POINTER(CpuParams), c_int, c_int, c_uint32,
                                      POINTER(c_int64), POINTER(c_int64), POINTER(c_int64)]
     lib.gor_cpu_baseline.restype = c_double
+    lib.gor_cpu_grid_baseline.argtypes = [c_int, POINTER(CpuParams), c_int, c_int, c_uint32,
+                                          POINTER(c_int64), POINTER(c_int64), POINTER(c_int64)]
+    lib.gor_cpu_grid_baseline.restype = c_double
     F32P, F64P = POINTER(c_float), POINTER(c_double)
     lib.gor_mlp_params.argtypes = []
     lib.gor_mlp_params.restype = c_int
@@ -117,6 +134,24 @@ def replay(sim: abi.SimParams, first: int, count: int, max_steps: int = 0):
     return st, steps, nrec, vals
 
 
+def replay_noise(sim: abi.SimParams, first: int, count: int, eps: float, on_increments: bool = False,
+                 max_steps: int = 0):
+    """replay() of a 2D model with a rounding-level perturbation of relative
+    size eps after every step, of r, theta and T (an uncompensated state) or
+    of the increments dr, dtheta, dT (a compensated state): the control that
+    measures how fast two replays differing at rounding level part."""
+    lib = load()
+    st = np.zeros(count, np.int32)
+    steps = np.zeros(count, np.uint32)
+    nrec = np.zeros(count, np.int32)
+    vals = np.zeros((count, 6), np.float64)
+    rc = lib.gor_replay_f64_noise(ctypes.byref(sim), first, count, max_steps, eps, int(on_increments),
+                                  st.ctypes.data_as(POINTER(c_int32)), steps.ctypes.data_as(POINTER(c_uint32)),
+                                  nrec.ctypes.data_as(POINTER(c_int32)), vals.ctypes.data_as(POINTER(c_double)))
+    assert rc == 0
+    return st, steps, nrec, vals
+
+
 def cpu_block(model: int, params: CpuParams, thread: int, threads: int, iteration: int, seed: int,
               max_rows: int = 100000):
     lib = load()
@@ -148,9 +183,28 @@ def cpu_baseline(model: int, params: CpuParams, threads: int, iterations: int, s
     return secs, nt.value, nr.value, ns.value
 
 
+def cpu_grid_baseline(model: int, cases, energies, per_point: int, threads: int, seed: int = 1):
+    """The reference CPU model's per-particle loop on a grid workload: every
+    parameter set in `cases` injects per_point particles at each of
+    `energies`; host threads take (case, energy) units dynamically.
+    Returns (seconds, trajectories, records, steps)."""
+    lib = load()
+    e = np.ascontiguousarray(energies, np.float32)
+    arr = (CpuParams * len(cases))()
+    for k, c in enumerate(cases):
+        ctypes.pointer(arr[k])[0] = c
+        arr[k].inj_energies = e.ctypes.data_as(POINTER(c_float))
+        arr[k].inj_points = e.size
+        arr[k].inj_per_point = per_point
+    nt, nr, ns = c_int64(), c_int64(), c_int64()
+    secs = lib.gor_cpu_grid_baseline(model, arr, len(cases), threads, seed, ctypes.byref(nt), ctypes.byref(nr),
+                                     ctypes.byref(ns))
+    return secs, nt.value, nr.value, ns.value
+
+
 def cpu_params_from_dict(d: dict) -> CpuParams:
     p = CpuParams()
-    for k, _ in CpuParams._fields_:
+    for k, _ in CpuParams._fields_[:11]:
         setattr(p, k, int(d[k]) if k == "useUniformInjection" else float(d[k]))
     return p
 

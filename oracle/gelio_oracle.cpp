@@ -137,6 +137,26 @@ float injection(const gelio_sim_params &p, uint64_t pid) {
   }
 }
 
+// Rounding-noise control: the relative perturbation (1 + eps s), s = +-1
+// drawn by a splitmix64 hash of (particle, step, variable).  Applied to r,
+// theta and T after every step of a 2D replay (noise_on_increments = 0) it
+// stands for one rounding of each state variable per step at relative
+// precision eps (an uncompensated state, as in the FP64 kernels); applied to
+// the increments dr, dtheta, dT instead (noise_on_increments = 1) it stands
+// for increments computed at relative precision eps added to a compensated
+// state (the FP32 kernels).  With eps = 0 the replay is the exact
+// restatement.  Test infrastructure only:
+// it measures how fast two replays that differ at rounding level part
+// (the 2D maps are chaotic near the poles and near r = 0).
+double noise_factor(double eps, uint64_t pid, uint32_t step, uint32_t var) {
+  if (eps == 0.0) return 1.0;
+  uint64_t z = pid * 0x9E3779B97F4A7C15ull + ((uint64_t)step << 2) + var + 0x632BE59BD9B4E019ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return (z & 1ull) ? 1.0 + eps : 1.0 - eps;
+}
+
 // ---------------------------------------------------------------------------
 // GPU flavour, one trajectory.  Literal FP64 restatement of the kernels.
 // ---------------------------------------------------------------------------
@@ -148,7 +168,8 @@ struct Traj {
   double Trec = 0, rrec = 0, auxrec = 0;
 };
 
-void gpu_geliosphere(const gelio_sim_params &p, uint64_t pid, uint64_t max_steps, Traj &t) {
+void gpu_geliosphere(const gelio_sim_params &p, uint64_t pid, uint64_t max_steps, Traj &t, double eps = 0.0,
+                     int noise_on_increments = 0) {
   const GpuK K;
   const uint32_t key[2] = {(uint32_t)p.seed, (uint32_t)(p.seed >> 32)};
   const double V = p.V, dt = p.dt, K0 = p.K0, ratio = p.ratio, delta0 = p.delta0;
@@ -248,9 +269,19 @@ void gpu_geliosphere(const gelio_sim_params &p, uint64_t pid, uint64_t max_steps
     DriftSheetR = polarity * konvF * (1.0 / (3.0 * A)) * Rig * beta * r * gamma * fprime / Cb;
     dr = dr + ((DriftR + DriftSheetR) * dt);
     dtheta = dtheta + (DriftTheta * dt / r);
+    if (eps != 0.0 && noise_on_increments) {
+      dr *= noise_factor(eps, pid, step, 0);
+      dtheta *= noise_factor(eps, pid, step, 1);
+      dTkin *= noise_factor(eps, pid, step, 2);
+    }
     r = r + dr;
     theta = theta + dtheta;
     Tkin = Tkin - dTkin;
+    if (eps != 0.0 && !noise_on_increments) {
+      r *= noise_factor(eps, pid, step, 0);
+      theta *= noise_factor(eps, pid, step, 1);
+      Tkin *= noise_factor(eps, pid, step, 2);
+    }
     if (theta < 0.0) theta = std::fabs(theta);
     if (theta > K.twoPi) theta = theta - K.twoPi;
     else if (theta > Pi) theta = K.twoPi - theta;
@@ -263,7 +294,8 @@ void gpu_geliosphere(const gelio_sim_params &p, uint64_t pid, uint64_t max_steps
   t.steps = step; t.T = Tkin; t.r = r; t.aux = theta;
 }
 
-void gpu_solarprop(const gelio_sim_params &p, uint64_t pid, uint64_t max_steps, Traj &t) {
+void gpu_solarprop(const gelio_sim_params &p, uint64_t pid, uint64_t max_steps, Traj &t, double eps = 0.0,
+                   int noise_on_increments = 0) {
   const GpuK K;
   const uint32_t key[2] = {(uint32_t)p.seed, (uint32_t)(p.seed >> 32)};
   const double V = p.V, dt = p.dt, K0 = p.K0, ratio = p.ratio, alphaM = p.tilt, polarity = p.polarity;
@@ -301,7 +333,7 @@ void gpu_solarprop(const gelio_sim_params &p, uint64_t pid, uint64_t max_steps, 
     double dtheta = (Ktt * cosineTheta) / (r * r * sineTheta);
     dtheta = (dtheta * dt) / (1.0 + gamma2);
     dtheta = dtheta + ((g1 * std::sqrt(2.0 * Ktt * dt)) / r);
-    const double dTkin = -2.0 * V * ((Tkin + T0 + T0) / (Tkin + T0)) * Tkin * dt / (3.0 * r);
+    double dTkin = -2.0 * V * ((Tkin + T0 + T0) / (Tkin + T0)) * Tkin * dt / (3.0 * r);
     const double Bfield = A * std::sqrt((1.0 + gamma2)) / (r * r);
     const double Larmor = 0.0225 * Rig / Bfield;
     double alphaH = Pi / std::sin(alphaM + (2.0 * Larmor * Pi / (r * 180.0)));
@@ -319,9 +351,19 @@ void gpu_solarprop(const gelio_sim_params &p, uint64_t pid, uint64_t max_steps, 
     dr = dr + ((DriftR + DriftSheetR) * dt);
     const double DriftTheta = dthc * Rig * beta * r * gamma * (2.0 + (gamma2)) * f / (g12);
     dtheta += (DriftTheta * dt / r);
+    if (eps != 0.0 && noise_on_increments) {
+      dr *= noise_factor(eps, pid, step, 0);
+      dtheta *= noise_factor(eps, pid, step, 1);
+      dTkin *= noise_factor(eps, pid, step, 2);
+    }
     r = r + dr;
     theta = theta + dtheta;
     Tkin = Tkin - dTkin;
+    if (eps != 0.0 && !noise_on_increments) {
+      r *= noise_factor(eps, pid, step, 0);
+      theta *= noise_factor(eps, pid, step, 1);
+      Tkin *= noise_factor(eps, pid, step, 2);
+    }
     if (theta < 0.0) theta = std::fabs(theta);
     if (theta > K.twoPi) theta = theta - K.twoPi;
     else if (theta > Pi) theta = K.twoPi - theta;
@@ -457,6 +499,12 @@ extern "C" struct gor_cpu_params {
   double V, dt, K0, ratio, delta0, alphaM, polarity, rInit, thetainj;
   int useUniformInjection;
   double uniformEnergyInjectionMaximum;
+  // Not in the reference: an injection grid for the 2D models' block loop.
+  // With inj_energies set, a block injects inj_per_point particles at each
+  // of the inj_points energies (in place of 500 at each of the 30 SolarProp
+  // energies); zero / null keeps the reference's injection.
+  const float *inj_energies;
+  int inj_points, inj_per_point;
 };
 
 namespace {
@@ -485,9 +533,11 @@ void cpu_geliosphere(const gor_cpu_params &c, int threadNumber, unsigned availab
   double dtheta, dTkin, delta, deltarh, deltarh2, DriftR, DriftTheta, arg, alphaH, Larmor, Bfield, f, fprime, DriftSheetR;
   double Kphph, Krt, Krph, Ktph, B11Temp, B11, B12, B13, B22, B23, sin2, sin3, dKtt1, dKtt2, dKrtr, dKrtt;
   int64_t steps = 0;
-  for (int energy = 0; energy < 30; energy++) {
-    for (int ppe = 0; ppe < 500; ppe++) {
-      Tkininj = (c.useUniformInjection)
+  const int n_energy = c.inj_energies ? c.inj_points : 30, n_ppe = c.inj_energies ? c.inj_per_point : 500;
+  for (int energy = 0; energy < n_energy; energy++) {
+    for (int ppe = 0; ppe < n_ppe; ppe++) {
+      Tkininj = c.inj_energies ? (double)c.inj_energies[energy]
+                : (c.useUniformInjection)
                     ? cpu_injection(((availableThreads * iteration + threadNumber) * 500) + ppe, 0.0001, c.uniformEnergyInjectionMaximum, 10000)
                     : kSPbins[energy];
       Tkin = Tkininj;
@@ -620,9 +670,11 @@ void cpu_solarprop(const gor_cpu_params &c, int threadNumber, unsigned available
   double w, r2, gamma, gamma2, onePlusGamma, onePlusGamma2, Kper, Krr, Tkinw, p, dtheta, dTkin;
   double DriftR, DriftTheta, arg, alphaH, Larmor, Bfield, f, fprime, DriftSheetR;
   int64_t steps = 0;
-  for (int energy = 0; energy < 30; energy++) {
-    for (int ppe = 0; ppe < 500; ppe++) {
-      Tkininj = (c.useUniformInjection)
+  const int n_energy = c.inj_energies ? c.inj_points : 30, n_ppe = c.inj_energies ? c.inj_per_point : 500;
+  for (int energy = 0; energy < n_energy; energy++) {
+    for (int ppe = 0; ppe < n_ppe; ppe++) {
+      Tkininj = c.inj_energies ? (double)c.inj_energies[energy]
+                : (c.useUniformInjection)
                     ? cpu_injection(((availableThreads * iteration + threadNumber) * 500) + ppe, 0.0001, c.uniformEnergyInjectionMaximum, 10000)
                     : kSPbins[energy];
       Tkin = Tkininj;
@@ -1010,6 +1062,27 @@ int gor_replay_f64(const gelio_sim_params *p, int64_t first, int64_t count, uint
   return 0;
 }
 
+// gor_replay_f64 of a 2D model with the rounding-noise control of relative
+// size eps applied after every step to r, theta and T (on_increments = 0) or
+// to dr, dtheta and dT (on_increments = 1); see noise_factor.
+int gor_replay_f64_noise(const gelio_sim_params *p, int64_t first, int64_t count, uint64_t max_steps,
+                         double eps, int32_t on_increments, int32_t *status, uint32_t *steps, int32_t *nrec,
+                         double *out6) {
+  if (!p || first < 0 || count < 0) return 1;
+  if (p->model != GELIO_MODEL_2D_GELIOSPHERE && p->model != GELIO_MODEL_2D_SOLARPROP) return 1;
+  if (max_steps == 0) max_steps = 100000000ull;
+  for (int64_t i = 0; i < count; ++i) {
+    Traj t;
+    const uint64_t pid = (uint64_t)(first + i);
+    if (p->model == GELIO_MODEL_2D_GELIOSPHERE) gpu_geliosphere(*p, pid, max_steps, t, eps, on_increments);
+    else gpu_solarprop(*p, pid, max_steps, t, eps, on_increments);
+    status[i] = t.status; steps[i] = t.steps; nrec[i] = t.nrec;
+    double *o = out6 + 6 * i;
+    o[0] = t.T; o[1] = t.r; o[2] = t.aux; o[3] = t.Trec; o[4] = t.rrec; o[5] = t.auxrec;
+  }
+  return 0;
+}
+
 // CPU flavour: one simulation(threadNumber, availableThreads, iteration) call
 // of the reference CPU model with a fresh std::mt19937(seed) and
 // std::normal_distribution<float>(0, 1).  Writes up to max_rows rows of
@@ -1065,6 +1138,46 @@ double gor_cpu_baseline(int model, const gor_cpu_params *c, int threads, int ite
   const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   const int64_t per_block = (model >= GELIO_MODEL_2D_SOLARPROP) ? 30 * 500 : 101 * 250;
   if (n_traj) *n_traj = per_block * (int64_t)threads * iterations;
+  if (n_records) *n_records = rec.load();
+  if (n_steps) *n_steps = st.load();
+  return secs;
+}
+
+// CPU baseline of a grid workload: the 2D model's reference CPU loop
+// (cpu flavour) over n_cases parameter sets, each injecting per_point
+// particles at every energy of params[k].inj_energies; host threads take
+// (case, grid point) units from a shared counter, each with its own
+// std::mt19937.  Returns wall seconds; n_traj / n_records / n_steps summed.
+double gor_cpu_grid_baseline(int model, const gor_cpu_params *params, int n_cases, int threads, uint32_t seed,
+                             int64_t *n_traj, int64_t *n_records, int64_t *n_steps) {
+  if (!params || n_cases < 1) return -1.0;
+  if (threads < 1) threads = (int)std::thread::hardware_concurrency();
+  if (threads < 1) threads = 1;
+  const int points = params[0].inj_points;
+  const int64_t units = (int64_t)n_cases * points;
+  std::atomic<int64_t> next{0}, rec{0}, st{0}, traj{0};
+  const auto t0 = std::chrono::steady_clock::now();
+  std::vector<std::thread> pool;
+  for (int t = 0; t < threads; ++t) {
+    pool.emplace_back([&, t]() {
+      std::mt19937 generator(seed + (uint32_t)t);
+      std::normal_distribution<float> distribution(0.0f, 1.0f);
+      for (int64_t u = next++; u < units; u = next++) {
+        gor_cpu_params c = params[u / points];
+        c.inj_energies = params[u / points].inj_energies + (u % points);
+        c.inj_points = 1;
+        RowSink sink{nullptr, 0, 0, cpu_cols(model)};
+        int64_t s = 0;
+        cpu_fn(model)(c, t, (unsigned)threads, 0, generator, distribution, sink, &s);
+        rec += sink.n;
+        st += s;
+        traj += c.inj_per_point;
+      }
+    });
+  }
+  for (auto &th : pool) th.join();
+  const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (n_traj) *n_traj = traj.load();
   if (n_records) *n_records = rec.load();
   if (n_steps) *n_steps = st.load();
   return secs;

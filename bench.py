@@ -14,7 +14,10 @@ e2e   : the same metric through gelio_run with host buffers (parameters
 --impl reference : the reference's CPU implementation of the path, run on
         this host's cores through the oracle port of the reference CPU model
         (the reference CPU code itself is pinned to it bit for bit, but its
-        sources are not available on this host).
+        sources are not available on this host), on the same workload: the
+        four cases, the same 100-point log grid with equal particles per
+        point (a bounded sample of it per step), so trajectories/s and
+        particle-steps/s are the same units of work in both arms.
 
 Other workloads (--workload; each prints its own line of the same form):
   bp        1D B-p, 1e7 protons on a 100-point log grid, FP32 steps (FP64
@@ -165,6 +168,11 @@ CONFIG = {
 }
 
 
+def headline_config(particles_per_case: int) -> dict:
+    """The `config` both arms of the headline print (the same workload)."""
+    return dict(CONFIG, particles_per_case=particles_per_case)
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle sampling during the timed region."""
 
@@ -219,33 +227,40 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_reference_params():
-    """Resolved statics of the reference CPU 2D Geliosphere model for the
-    workload (its own SolarProp injection grid; tilt 20 deg, A>0)."""
-    import numpy as np
+def cpu_case_params(sim):
+    """Resolved statics of the reference CPU 2D Geliosphere model
+    (Constants.hpp setContants) for one case of the workload: the case's own
+    K0, V, dt, tilt, polarity, r and theta, as the GPU run uses them."""
     from oracle import ffi
-    f32 = np.float32
     p = ffi.CpuParams()
-    p.V = float(f32(float(f32(400.0)) * 6.68458712e-9))
-    p.dt = 500.0
-    p.K0 = float(f32(float(f32(5e22)) * 4.4683705e-27))
-    p.ratio = float(f32(0.2))
-    p.delta0 = float(f32(8.7e-5))
-    p.alphaM = float(f32(f32(f32(20.0) * f32(3.1415926535)) / f32(180.0)))
-    p.polarity = 1.0
-    p.rInit = 1.0
-    p.thetainj = float(f32(f32(f32(90.0) * f32(3.1415926535)) / f32(180.0)))
+    p.V, p.dt, p.K0 = float(sim.V), float(sim.dt), float(sim.K0)
+    p.ratio, p.delta0 = float(sim.ratio), float(sim.delta0)
+    p.alphaM, p.polarity = float(sim.tilt), float(sim.polarity)
+    p.rInit, p.thetainj = float(sim.r_injection), float(sim.theta_injection)
     p.useUniformInjection = 0
     p.uniformEnergyInjectionMaximum = 101.0
     return p
 
 
-def cpu_baseline_sample(threads: int):
-    """One iteration of the reference CPU model structure on `threads` host
-    threads (30 energies x 500 particles each)."""
+# particles per grid point and case of one CPU sample (4 cases x 100 points)
+CPU_SAMPLE_PER_POINT = {"cpu_baseline": 32, "reference_step": 16}
+
+
+def cpu_baseline_sample(threads: int, per_point: int):
+    """A bounded sample of the headline workload on the reference CPU model's
+    per-particle loop (the oracle port, pinned to it bit for bit): the four
+    cases, `per_point` particles at each of the 100 log-grid energies of
+    each, host threads taking (case, energy) units dynamically.  Returns
+    (seconds, trajectories, records, particle-steps)."""
     from oracle import ffi
-    secs, ntraj, nrec, nsteps = ffi.cpu_baseline(3, cpu_reference_params(), threads, 1, seed=1)
-    return secs, ntraj, nrec, nsteps
+    sims = workload_sims(1, 0)
+    energies = [ffi.injection(sims[0], i) for i in range(sims[0].inj_points)]
+    return ffi.cpu_grid_baseline(3, [cpu_case_params(s) for s in sims], energies, per_point, threads, seed=1)
+
+
+def cpu_sample_text(threads: int, per_point: int, ntraj: int, secs: float) -> str:
+    return ("%d trajectories of the same workload (4 cases x 100 log-grid energies x %d particles), reference "
+            "CPU model loop (FP64 oracle port) on %d host threads, %.2f s" % (ntraj, per_point, threads, secs))
 
 
 # bounded CPU samples of the 1D workloads: (chunks, contiguous particles per
@@ -322,23 +337,25 @@ def run_reference(args, rank, world):
     from oracle import ffi
     ffi.build()
     threads = os.cpu_count() or 1
+    per = CPU_SAMPLE_PER_POINT["reference_step"]
     for _ in range(args.warmup):
-        cpu_baseline_sample(threads)
-    tot_s, tot_traj = 0.0, 0
+        cpu_baseline_sample(threads, per)
+    tot_s, tot_traj, tot_steps = 0.0, 0, 0
     for _ in range(args.steps):
-        s, n, _, _ = cpu_baseline_sample(threads)
+        s, n, _, st = cpu_baseline_sample(threads, per)
         tot_s += s
         tot_traj += n
+        tot_steps += st
     v = tot_traj / tot_s
+    sample = cpu_sample_text(threads, per, tot_traj // args.steps, tot_s / args.steps)
     line = {
         "metric": "2D Geliosphere trajectories/s", "value": v, "unit": "trajectories/s", "impl": "reference",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_s / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": dict(CONFIG, sample="one iteration of the reference CPU model per step: %d threads x 30 "
-                                      "energies x 500 particles (its own 30-point SolarProp grid, tilt 20, A>0)"
-                                      % threads),
+        "config": headline_config(args.particles or CONFIG["particles_per_case"]),
+        "particle_steps_per_s": tot_steps / tot_s,
         "cpu_baseline": {"value": v, "unit": "trajectories/s", "cores": threads, "kind": "port",
-                         "sample": "%d trajectories per step" % (tot_traj // args.steps)},
+                         "sample": sample},
         "e2e": {"value": v, "unit": "trajectories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -720,12 +737,14 @@ def main():
     steps_per_s = steps_per_run / (k_ms / 1e3)
     achieved_tflops = steps_per_s * ALG_FLOP_PER_STEP / 1e12
     achieved_xu = steps_per_s * ALG_XU_PER_STEP / 1e9
-    traffic = None
+    traffic, issue = None, None
     tfile = os.path.join(ROOT, "profiles", "k_persistent_geliosphere_fp32_dram.txt")
     if os.path.exists(tfile):
         for ln in open(tfile):
             if ln.startswith("dram_bytes_per_launch:"):
                 traffic = float(ln.split(":")[1])
+            if ln.startswith("issue_slots_busy_frac:"):
+                issue = float(ln.split(":")[1])
     line = {
         "metric": "2D Geliosphere trajectories/s",
         "value": value,
@@ -739,8 +758,8 @@ def main():
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": dict(CONFIG, particles_per_case=args.particles,
-                       tuned={"block": tune.block_size, "refill": tune.refill_interval} if tune else None),
+        "config": headline_config(args.particles),
+        "tuned": {"block": tune.block_size, "refill": tune.refill_interval} if tune else None,
         "particle_steps_per_s": steps_per_s,
         "e2e": {"value": e2e_value, "unit": "trajectories/s",
                 "h2d_bytes_per_step": n * ctypes.sizeof(abi.SimParams),
@@ -760,6 +779,10 @@ def main():
             "kernel": "k_persistent<2D Geliosphere, float>",
             "kernel_ms": k_ms,
             "alg_xu_per_particle_step": ALG_XU_PER_STEP,
+            # what the hardware ran: ncu's issue-slot utilisation of the same
+            # kernel (the kernel is issue-bound; the SFU fraction above
+            # counts the reference step's special-function work)
+            "issue_slots_busy_frac": issue,
             "peak_source": "measured in this run by gelio_measure_peaks (ex2.approx chains, special-function "
                            "unit; FP32 FMA chains); MEASURED_PEAKS.json holds no SFU or FP32 SIMT figure",
             "fp32": {"achieved_tflops": achieved_tflops, "peak_tflops": fp32_tflops,
@@ -771,11 +794,11 @@ def main():
         from oracle import ffi
         ffi.build()
         threads = os.cpu_count() or 1
-        secs, ntraj, nrec, nsteps = cpu_baseline_sample(threads)
+        per = CPU_SAMPLE_PER_POINT["cpu_baseline"]
+        secs, ntraj, nrec, nsteps = cpu_baseline_sample(threads, per)
         line["cpu_baseline"] = {"value": ntraj / secs, "unit": "trajectories/s", "cores": threads, "kind": "port",
-                                "sample": "%d trajectories: one iteration of the reference CPU 2D Geliosphere "
-                                          "model structure (%d threads x 30 energies x 500 particles, its "
-                                          "30-point SolarProp grid, tilt 20, A>0), %.1f s" % (ntraj, threads, secs)}
+                                "particle_steps_per_s": nsteps / secs,
+                                "sample": cpu_sample_text(threads, per, ntraj, secs)}
     print(json.dumps(line), flush=True)
     eng.close()
     if world > 1:

@@ -37,9 +37,9 @@ K0_AU = float(np.float32(float(np.float32(5e22)) * 4.4683705e-27))       # Input
 V_AU = float(np.float32(float(np.float32(400.0)) * 6.68458712e-9))       # InputValidation::setV
 
 
-def base_args(dt, tilt=20, polarity=1, uniform=0):
+def base_args(dt, tilt=20, polarity=1, uniform=0, r=1, theta=90):
     return [f"dt={dt}", f"K0={K0_AU!r}", "K0_entered_by_user=1", f"V={V_AU!r}", f"tilt_angle={tilt}",
-            f"polarity={polarity}", "r_injection=1", "theta_injection=90", "geliosphereRatio=0.2",
+            f"polarity={polarity}", f"r_injection={r}", f"theta_injection={theta}", "geliosphereRatio=0.2",
             "solarPropRatio=0.02", "C_delta=8.7e-05", f"use_uniform_injection={uniform}"]
 
 
@@ -194,6 +194,20 @@ def spectra_goldens():
         # + 0..249, each 101 times, so 8,080 blocks cover the CPU grid's
         # 1,010,000 ids exactly twice (a uniform injection spectrum)
         "fp_dt50": ("fp", base_args(50), 8080),
+        # the other two (polarity, tilt) cases of the four-case 2D workload
+        "geliosphere_a_pos_tilt70": ("geliosphere", base_args(500, tilt=70, polarity=1), 48),
+        "geliosphere_a_neg_tilt20": ("geliosphere", base_args(500, tilt=20, polarity=-1), 48),
+        # off-equator injections beyond 1 AU from the batch ranges (r 1-80 AU,
+        # theta 10-170 deg); "uni" cases inject on the CPU models' linear
+        # 1e4-point grid up to 101 GeV (use_uniform_injection), so the AMS and
+        # Ulysses bins see continuous energies.  40 blocks of 500 ids cover
+        # that grid exactly twice.
+        "geliosphere_r5_th30_a_pos_tilt20_uni": ("geliosphere", base_args(500, 20, 1, 1, r=5, theta=30), 40),
+        "geliosphere_r30_th120_a_neg_tilt45": ("geliosphere", base_args(500, 45, -1, 0, r=30, theta=120), 48),
+        "geliosphere_r70_th160_a_pos_tilt70_uni": ("geliosphere", base_args(500, 70, 1, 1, r=70, theta=160), 40),
+        "solarprop_r5_th30_a_neg_tilt20": ("solarprop", base_args(500, 20, -1, 0, r=5, theta=30), 48),
+        "solarprop_r30_th120_a_pos_tilt45_uni": ("solarprop", base_args(500, 45, 1, 1, r=30, theta=120), 40),
+        "solarprop_r70_th160_a_neg_tilt70": ("solarprop", base_args(500, 70, -1, 0, r=70, theta=160), 48),
     }
     only = [a.split("=", 1)[1].split(",") for a in sys.argv if a.startswith("--spectra=")]
     for name, (model, args, nb) in cases.items():

@@ -36,7 +36,9 @@ def sim_from_fixture(doc, n, seed):
     p.delta0 = r["delta0"]
     p.injection_max = r["uniformEnergyInjectionMaximum"]
     if model >= 2:
-        p.injection = abi.GELIO_INJ_SOLARPROP_GRID
+        # use_uniform_injection picks the CPU models' linear 1e4-point grid
+        # (GeliosphereCpuModel.cpp:81-83), else the SolarProp 30-point grid
+        p.injection = abi.GELIO_INJ_CPU_UNIFORM if r["useUniformInjection"] else abi.GELIO_INJ_SOLARPROP_GRID
         # the CPU model uses the polarity in the SolarProp theta drift
         p.flags = abi.GELIO_FLAG_SOLARPROP_THETA_DRIFT_POLARITY
     else:
@@ -62,30 +64,41 @@ def compare_sections(gpu, ref, sections, min_count=200):
     return np.concatenate(zs)
 
 
-@pytest.mark.parametrize("case", ["geliosphere_a_pos_tilt20", "geliosphere_a_neg_tilt70", "solarprop_a_pos",
-                                  "solarprop_a_neg_tilt70"])
+TWO_D_CASES = sorted(os.path.basename(f)[len("ref_spectra_"):-len(".json")]
+                     for f in os.listdir(GOLDEN) if f.startswith("ref_spectra_") and
+                     f.startswith(("ref_spectra_geliosphere", "ref_spectra_solarprop")))
+
+
+@pytest.mark.parametrize("case", TWO_D_CASES)
 def test_2d_spectra_match_reference_cpu_model(engine, case):
-    path = os.path.join(GOLDEN, f"ref_spectra_{case}.json")
-    if not os.path.exists(path):
-        pytest.skip("fixture not generated")
-    doc = json.load(open(path))
+    """Every 2D reference fixture: the four (polarity, tilt) cases of the 2D
+    workload at r 1 AU, theta 90 deg, and injections off the equator and
+    beyond 1 AU (r 5-70 AU, theta 30-160 deg) for both 2D models, on the
+    SolarProp grid or on the CPU models' linear grid ("_uni").  Compared:
+    the SolarProp section (three LIS), the Ulysses bins and the AMS bins."""
+    doc = json.load(open(os.path.join(GOLDEN, f"ref_spectra_{case}.json")))
     sim = sim_from_fixture(doc, 3_000_000, seed=2024)
     gpu = spectra_dict(engine.run(sim).spectra[0])
     ref = doc["spectra"]
-    z = compare_sections(gpu, ref, [("sp_weber", "sp_weber2", "sp_n"), ("sp_jgr", "sp_jgr2", "sp_n"),
-                                    ("sp_burger", "sp_burger2", "sp_n")])
-    assert z.size >= 60
-    # per-bin mean weights within Monte Carlo error (the three LIS share the
-    # particles, so chi^2/dof is taken over the Weber bins).  Tolerances: the
-    # target chi^2/dof <= 1.2; max |z| < 3.5 over the 87 correlated
-    # comparisons (a 3-sigma excursion in one of them is expected a few % of
-    # the time by chance).
-    zb = z[: z.size // 3]
-    chi2_dof = float(np.mean(zb ** 2))
-    print(f"{case}: bins {zb.size}, max|z| {np.abs(z).max():.2f}, chi2/dof {chi2_dof:.3f}, "
-          f"within 3 sigma {np.mean(np.abs(z) < 3):.3f}")
-    assert np.abs(z).max() < 3.5
-    assert chi2_dof <= 1.2
+    sections = {"weber": ("sp_weber", "sp_weber2", "sp_n"), "jgr": ("sp_jgr", "sp_jgr2", "sp_n"),
+                "burger": ("sp_burger", "sp_burger2", "sp_n"), "ulysses": ("uly_w", "uly_w2", "uly_n"),
+                "ams": ("ams_w", "ams_w2", "ams_n")}
+    z = {k: compare_sections(gpu, ref, [v]) for k, v in sections.items()}
+    zall = np.concatenate(list(z.values()))
+    # per-bin mean weights within Monte Carlo error.  chi^2/dof over the
+    # Weber bins of the SolarProp section (the three LIS share the particles,
+    # and on the SolarProp grid the Ulysses and AMS bins hold the same
+    # particles as SolarProp bins), and over the AMS bins when they see a
+    # continuous injection spectrum; max |z| < 3.5 over every comparison.
+    chi2 = {"weber": float(np.mean(z["weber"] ** 2))}
+    if z["ams"].size >= 20:
+        chi2["ams"] = float(np.mean(z["ams"] ** 2))
+    print(f"{case}: bins " + " ".join(f"{k} {v.size}" for k, v in z.items()) +
+          f"; max|z| {np.abs(zall).max():.2f}; chi2/dof " + " ".join(f"{k} {v:.3f}" for k, v in chi2.items()) +
+          f"; within 3 sigma {np.mean(np.abs(zall) < 3):.3f}")
+    assert z["weber"].size >= 12 and z["ams"].size >= 5 and z["ulysses"].size >= 1
+    assert np.abs(zall).max() < 3.5
+    assert max(chi2.values()) <= 1.2
 
 
 def test_bp_spectra_match_reference_cpu_model(engine):

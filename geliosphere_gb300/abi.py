@@ -134,6 +134,11 @@ assert ctypes.sizeof(RunStats) == 88
 assert ctypes.sizeof(Trajectory) == 40
 assert ctypes.sizeof(SurrogateOpts) == 80
 
+# gelio_set_alloc_hook: kinds and the hook's C signature
+GELIO_ALLOC_DEVICE = 0
+GELIO_ALLOC_PINNED_HOST = 1
+ALLOC_HOOK = ctypes.CFUNCTYPE(c_int32, c_int32, c_uint64, c_void_p)
+
 # C-ABI entry points declared in include/gelio.h: name -> (restype, argtypes)
 PROTOTYPES = {
     "gelio_status_string": (ctypes.c_char_p, [c_int32]),
@@ -151,6 +156,7 @@ PROTOTYPES = {
                                  POINTER(Spectra)]),
     "gelio_autotune": (c_int32, [c_void_p, POINTER(SimParams), c_int32, POINTER(RunOpts)]),
     "gelio_measure_peaks": (c_int32, [c_void_p, POINTER(c_double), POINTER(c_double)]),
+    "gelio_set_alloc_hook": (c_int32, [ALLOC_HOOK, c_void_p]),
     "gelio_run_noalloc": (c_int32, [c_void_p, c_int32, POINTER(RunOpts), c_void_p, c_void_p]),
     "gelio_surrogate_create": (c_int32, [c_void_p, POINTER(SurrogateOpts), POINTER(c_void_p)]),
     "gelio_surrogate_destroy": (None, [c_void_p]),

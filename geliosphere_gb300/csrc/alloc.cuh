@@ -1,0 +1,22 @@
+// Device and pinned-host allocations of the engine, routed through the
+// process-wide allocation hook of gelio_set_alloc_hook (include/gelio.h):
+// a hook that refuses an allocation makes it fail with
+// cudaErrorMemoryAllocation without calling CUDA, exactly as an exhausted
+// device would, so callers report GELIO_ERR_OUT_OF_MEMORY.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstddef>
+
+namespace gelio {
+
+cudaError_t dev_malloc_raw(void **p, size_t bytes);
+cudaError_t pinned_malloc_raw(void **p, size_t bytes);
+
+template <class T> inline cudaError_t dev_malloc(T **p, size_t bytes) {
+  return dev_malloc_raw(reinterpret_cast<void **>(p), bytes);
+}
+template <class T> inline cudaError_t pinned_malloc(T **p, size_t bytes) {
+  return pinned_malloc_raw(reinterpret_cast<void **>(p), bytes);
+}
+
+}  // namespace gelio

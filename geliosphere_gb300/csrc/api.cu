@@ -11,6 +11,7 @@
 // prepareAndRunSimulation call (e.g. GeliosphereGpuModel.cpp:17-43) and
 // synchronises three times per 4,096-particle chunk.
 #include <cuda_runtime.h>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -20,9 +21,32 @@
 #include <vector>
 
 #include "gelio.h"
+#include "alloc.cuh"
 #include "kernels.cuh"
 
 namespace gelio {
+
+// ---------------------------------------------------------------------------
+// Allocation hook (gelio_set_alloc_hook): consulted before every device and
+// pinned-host allocation of the engine.
+// ---------------------------------------------------------------------------
+static std::atomic<gelio_alloc_hook> g_alloc_hook{nullptr};
+static std::atomic<void *> g_alloc_user{nullptr};
+
+static bool alloc_refused(int32_t kind, size_t bytes) {
+  const gelio_alloc_hook h = g_alloc_hook.load();
+  return h != nullptr && h(kind, (uint64_t)bytes, g_alloc_user.load()) != 0;
+}
+
+cudaError_t dev_malloc_raw(void **p, size_t bytes) {
+  if (alloc_refused(GELIO_ALLOC_DEVICE, bytes)) { *p = nullptr; return cudaErrorMemoryAllocation; }
+  return cudaMalloc(p, bytes);
+}
+
+cudaError_t pinned_malloc_raw(void **p, size_t bytes) {
+  if (alloc_refused(GELIO_ALLOC_PINNED_HOST, bytes)) { *p = nullptr; return cudaErrorMemoryAllocation; }
+  return cudaMallocHost(p, bytes);
+}
 
 cudaError_t fp_launch(bool, int, unsigned, unsigned, size_t, cudaStream_t, const KArgs &);
 cudaError_t bp_launch(bool, int, unsigned, unsigned, size_t, cudaStream_t, const KArgs &);
@@ -343,7 +367,7 @@ struct gelio_ctx {
   // graph cache
   cudaGraphExec_t graph = nullptr;
   unsigned long long graph_key[8] = {0};
-  const void *graph_out = nullptr;
+  const void *graph_bufs[12] = {};     // buffer addresses the cached graph was captured with
   // tuning and last run
   Tuned tuned[4][2];
   int occ_cache[4][3][8][5] = {};   // [model][kernel variant][block/32 - 1][smem slots]
@@ -379,7 +403,7 @@ static cudaError_t grow(T *&ptr, size_t &cap_bytes, size_t need_bytes) {
   if (ptr) cudaFree(ptr);
   ptr = nullptr;
   cap_bytes = 0;
-  cudaError_t e = cudaMalloc((void **)&ptr, need_bytes);
+  cudaError_t e = dev_malloc(&ptr, need_bytes);
   if (e == cudaSuccess) cap_bytes = need_bytes;
   return e;
 }
@@ -404,11 +428,11 @@ static int ensure_sims(gelio_ctx *c, int n) {
   cudaFree(c->d_params); cudaFree(c->d_sims); cudaFree(c->d_tables); cudaFree(c->d_gsim); cudaFree(c->d_gpre);
   c->d_params = nullptr; c->d_sims = nullptr; c->d_tables = nullptr; c->d_gsim = nullptr; c->d_gpre = nullptr;
   c->cap_sims = 0;
-  GELIO_TRY(cudaMalloc(&c->d_params, sizeof(gelio_sim_params) * cap));
-  GELIO_TRY(cudaMalloc(&c->d_sims, sizeof(SimDev) * cap));
-  GELIO_TRY(cudaMalloc(&c->d_tables, sizeof(float) * GELIO_GRID_MAX * cap));
-  GELIO_TRY(cudaMalloc(&c->d_gsim, sizeof(int) * 4 * cap));
-  GELIO_TRY(cudaMalloc(&c->d_gpre, sizeof(unsigned long long) * 4 * (cap + 1)));
+  GELIO_TRY(dev_malloc(&c->d_params, sizeof(gelio_sim_params) * cap));
+  GELIO_TRY(dev_malloc(&c->d_sims, sizeof(SimDev) * cap));
+  GELIO_TRY(dev_malloc(&c->d_tables, sizeof(float) * GELIO_GRID_MAX * cap));
+  GELIO_TRY(dev_malloc(&c->d_gsim, sizeof(int) * 4 * cap));
+  GELIO_TRY(dev_malloc(&c->d_gpre, sizeof(unsigned long long) * 4 * (cap + 1)));
   c->cap_sims = cap;
   if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
   return GELIO_OK;
@@ -539,8 +563,8 @@ int32_t gelio_create(gelio_ctx **out, int32_t device) {
     if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) { rc = map_cuda(e); break; }
     if ((e = cudaEventCreate(&c->ev_k0)) != cudaSuccess) { rc = map_cuda(e); break; }
     if ((e = cudaEventCreate(&c->ev_k1)) != cudaSuccess) { rc = map_cuda(e); break; }
-    if ((e = cudaMalloc(&c->d_ctl, sizeof(Control))) != cudaSuccess) { rc = map_cuda(e); break; }
-    if ((e = cudaMallocHost(&c->h_ctl, sizeof(Control))) != cudaSuccess) { rc = map_cuda(e); break; }
+    if ((e = dev_malloc(&c->d_ctl, sizeof(Control))) != cudaSuccess) { rc = map_cuda(e); break; }
+    if ((e = pinned_malloc(&c->h_ctl, sizeof(Control))) != cudaSuccess) { rc = map_cuda(e); break; }
     BinTables t;
     build_tables(t);
     if ((e = fp_tables(t)) != cudaSuccess || (e = bp_tables(t)) != cudaSuccess ||
@@ -684,7 +708,7 @@ int32_t gelio_run(gelio_ctx *c, const gelio_sim_params *sims, int32_t n, const g
     if (c->h_params) cudaFreeHost(c->h_params);
     c->h_params = nullptr;
     c->h_params_cap = 0;
-    GELIO_TRY(cudaMallocHost(&c->h_params, sizeof(gelio_sim_params) * c->cap_sims));
+    GELIO_TRY(pinned_malloc(&c->h_params, sizeof(gelio_sim_params) * c->cap_sims));
     c->h_params_cap = c->cap_sims;
   }
   memcpy(c->h_params, sims, sizeof(gelio_sim_params) * n);
@@ -712,18 +736,24 @@ int32_t gelio_run(gelio_ctx *c, const gelio_sim_params *sims, int32_t n, const g
     c->h_out = nullptr;
     c->h_out_cap = 0;
     if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
-    GELIO_TRY(cudaMallocHost(&c->h_out, sizeof(gelio_spectra) * c->cap_sims));
+    GELIO_TRY(pinned_malloc(&c->h_out, sizeof(gelio_spectra) * c->cap_sims));
     c->h_out_cap = c->cap_sims;
   }
   if (graph) {
     // graphs copy through pinned staging (pageable host memory cannot be a
     // memcpy node); the staging pointer is fixed, so the graph is reusable
-    const bool hit = c->graph && memcmp(key, c->graph_key, sizeof(key)) == 0 && c->graph_out == c->h_out;
+    // buffers the run grows lazily are grown here: no allocation may happen
+    // while the stream is being captured
+    GELIO_TRY(grow(c->d_part, c->part_bytes, (size_t)choose_slices(n) * n * kSpecDoubles * 8));
+    // a cached graph holds the addresses it was captured with: any buffer
+    // regrown since (by a run of another size, or after a refused
+    // allocation) makes it stale
+    const void *bufs[12] = {c->d_params, c->d_sims, c->d_tables, c->d_gsim, c->d_gpre, c->d_ctl,
+                            c->d_part, c->d_out, c->d_rec, c->h_params, c->h_out, c->h_ctl};
+    const bool hit = c->graph && memcmp(key, c->graph_key, sizeof(key)) == 0 &&
+                     memcmp(bufs, c->graph_bufs, sizeof(bufs)) == 0;
     if (!hit) {
       if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
-      // buffers the run grows lazily are grown here: no allocation may
-      // happen while the stream is being captured
-      GELIO_TRY(grow(c->d_part, c->part_bytes, (size_t)choose_slices(n) * n * kSpecDoubles * 8));
       cudaGraph_t gr;
       GELIO_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
       cudaError_t e = cudaMemcpyAsync(c->d_params, c->h_params, sizeof(gelio_sim_params) * n,
@@ -741,7 +771,7 @@ int32_t gelio_run(gelio_ctx *c, const gelio_sim_params *sims, int32_t n, const g
       cudaGraphDestroy(gr);
       GELIO_TRY(e);
       memcpy(c->graph_key, key, sizeof(key));
-      c->graph_out = c->h_out;
+      memcpy(c->graph_bufs, bufs, sizeof(bufs));
     }
     GELIO_TRY(cudaGraphLaunch(c->graph, st));
   } else {
@@ -890,12 +920,18 @@ int32_t gelio_evaluate(gelio_ctx *c, int32_t model, const double *rows, int64_t 
   return GELIO_OK;
 }
 
+int32_t gelio_set_alloc_hook(gelio_alloc_hook hook, void *user) {
+  g_alloc_user.store(user);
+  g_alloc_hook.store(hook);
+  return GELIO_OK;
+}
+
 int32_t gelio_measure_peaks(gelio_ctx *c, double *fp32_tflops, double *xu_gops) {
   if (!c || !fp32_tflops || !xu_gops) return GELIO_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lock(c->mu);
   GELIO_TRY(cudaSetDevice(c->device));
   float *d = nullptr;
-  GELIO_TRY(cudaMalloc(&d, sizeof(float)));
+  GELIO_TRY(dev_malloc(&d, sizeof(float)));
   const unsigned grid = (unsigned)c->sm_count * 8u, block = 256u;
   const int it_f = 2048, it_x = 512;
   float best_f = 1e30f, best_x = 1e30f;

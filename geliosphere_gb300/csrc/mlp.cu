@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "gelio.h"
+#include "alloc.cuh"
 #include "mlp_kernels.cuh"
 
 int gelio_internal_device(const gelio_ctx *c);
@@ -309,8 +310,8 @@ int infer_rows(gelio_surrogate *s, int m0, int m1, const float *x, size_t n, flo
     if (s->d_yq) cudaFree(s->d_yq);
     s->d_query = s->d_yq = nullptr;
     s->query_cap = 0;
-    SUR_TRY(cudaMalloc(&s->d_query, n * kFeatures * 4));
-    SUR_TRY(cudaMalloc(&s->d_yq, n * 16 * 4));
+    SUR_TRY(gelio::dev_malloc(&s->d_query, n * kFeatures * 4));
+    SUR_TRY(gelio::dev_malloc(&s->d_yq, n * 16 * 4));
     s->query_cap = n;
   }
   SUR_TRY(cudaMemcpyAsync(s->d_query, x, n * kFeatures * 4, cudaMemcpyHostToDevice, s->stream));
@@ -413,7 +414,7 @@ int32_t gelio_surrogate_create(gelio_ctx *ctx, const gelio_surrogate_opts *opts,
   const size_t R = (size_t)s->rows;
   auto alloc = [&](void **p, size_t bytes) {
     if (rc != GELIO_OK) return;
-    cudaError_t e = cudaMalloc(p, bytes);
+    cudaError_t e = gelio::dev_malloc(p, bytes);
     if (e == cudaSuccess) e = cudaMemset(*p, 0, bytes);
     rc = cuda_status(e);
   };
@@ -560,8 +561,8 @@ int32_t gelio_surrogate_train(gelio_surrogate *s, int32_t epochs, float *last_lo
       if (s->d_feats) cudaFree(s->d_feats);
       if (s->d_targ) cudaFree(s->d_targ);
       s->d_feats = s->d_targ = nullptr;
-      SUR_TRY(cudaMalloc(&s->d_feats, nrow * kFeatures * 4));
-      SUR_TRY(cudaMalloc(&s->d_targ, nrow * 4));
+      SUR_TRY(gelio::dev_malloc(&s->d_feats, nrow * kFeatures * 4));
+      SUR_TRY(gelio::dev_malloc(&s->d_targ, nrow * 4));
       s->d_rows_cap = nrow;
     }
     SUR_TRY(cudaMemcpy(s->d_feats, s->feats.data(), nrow * kFeatures * 4, cudaMemcpyHostToDevice));
@@ -574,13 +575,13 @@ int32_t gelio_surrogate_train(gelio_surrogate *s, int32_t epochs, float *last_lo
   if (steps > s->step_loss_cap) {
     if (s->step_loss) cudaFree(s->step_loss);
     s->step_loss = nullptr;
-    SUR_TRY(cudaMalloc(&s->step_loss, sizeof(float) * steps));
+    SUR_TRY(gelio::dev_malloc(&s->step_loss, sizeof(float) * steps));
     s->step_loss_cap = steps;
   }
   if (nrow > s->order_cap) {
     if (s->order) cudaFree(s->order);
     s->order = nullptr;
-    SUR_TRY(cudaMalloc(&s->order, nrow * sizeof(int)));
+    SUR_TRY(gelio::dev_malloc(&s->order, nrow * sizeof(int)));
     s->order_cap = nrow;
   }
   const long long total = (long long)epochs * steps;
@@ -643,8 +644,8 @@ int32_t gelio_surrogate_gradient(gelio_surrogate *s, int32_t member, const float
   SUR_TRY(cudaSetDevice(s->device));
   float *d_x = nullptr, *d_t = nullptr, *d_loss = nullptr;
   int rc = GELIO_OK;
-  if (cudaMalloc(&d_x, (size_t)n * kFeatures * 4) != cudaSuccess || cudaMalloc(&d_t, (size_t)n * 4) != cudaSuccess ||
-      cudaMalloc(&d_loss, 4) != cudaSuccess)
+  if (gelio::dev_malloc(&d_x, (size_t)n * kFeatures * 4) != cudaSuccess || gelio::dev_malloc(&d_t, (size_t)n * 4) != cudaSuccess ||
+      gelio::dev_malloc(&d_loss, 4) != cudaSuccess)
     rc = GELIO_ERR_OUT_OF_MEMORY;
   if (rc == GELIO_OK && (cudaMemcpyAsync(d_x, x, (size_t)n * kFeatures * 4, cudaMemcpyHostToDevice, s->stream) !=
                              cudaSuccess ||

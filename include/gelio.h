@@ -241,6 +241,22 @@ typedef struct gelio_ctx gelio_ctx;
 const char *gelio_status_string(int32_t status);
 int32_t gelio_abi_version(void);
 
+/* Allocation hook.  No counterpart in the reference: its GpuModel classes
+ * allocate with cudaMallocManaged / cudaMalloc / cudaMallocHost inside each
+ * prepareAndRunSimulation (e.g. CUDAKernel/src/GeliosphereGpuModel.cpp:
+ * 17-22), and a failed allocation ends the process through gpuErrchk
+ * (CUDAKernel/include/CudaErrorCheck.cuh:31-41).  Here every device and
+ * pinned-host allocation the engine makes (contexts, surrogates) first calls
+ * hook(kind, bytes, user); a nonzero return refuses it, and the call that
+ * needed the memory returns GELIO_ERR_OUT_OF_MEMORY, as on an exhausted
+ * device: no memory is taken, and the context or surrogate stays usable (a
+ * later call allocates again).  This lets a host application hold the
+ * engine to a memory budget.  One hook per process; NULL removes it.  The
+ * hook may run on any thread that calls the engine and must not call it. */
+enum { GELIO_ALLOC_DEVICE = 0, GELIO_ALLOC_PINNED_HOST = 1 };
+typedef int32_t (*gelio_alloc_hook)(int32_t kind, uint64_t bytes, void *user);
+int32_t gelio_set_alloc_hook(gelio_alloc_hook hook, void *user);
+
 /* Text of the last CUDA failure on the calling thread (empty if none):
  * the CUDA error name and message and where it was raised.  Diagnostics
  * only; the status codes are the contract. */
@@ -303,12 +319,16 @@ int32_t gelio_autotune(gelio_ctx *ctx, const gelio_sim_params *sims, int32_t n,
  * array of GELIO_NOALLOC_SCRATCH_BYTES that every GPU loading the library
  * holds until the process exits.  The first call on a device sets that
  * device up (resolves the array's address, fills tables, queries
- * occupancy), so it should be made before any stream capture.  Calls share the
- * array: calls that overlap on the GPU (other streams, other threads) race
- * and corrupt each other.  The call waits for its own work on `stream` and
- * returns its status.  Exit records and the plain kernel are not available
- * here (GELIO_ERR_UNSUPPORTED); more than GELIO_NOALLOC_MAX_SIMS simulations
- * is GELIO_ERR_INVALID_ARGUMENT. */
+ * occupancy), so it should be made before any stream capture; a set-up that
+ * fails is retried by the next call, and after a cudaDeviceReset the process
+ * must be restarted before this entry point is called again.  Calls share
+ * the array: calls that overlap on the GPU (other streams, other threads)
+ * race and corrupt each other.  The call waits for its own work on `stream`
+ * and returns its status.  Of the options, precision, refill_interval,
+ * max_steps_per_particle and time_limit_s apply; exit records, the plain
+ * kernel and any other launch shape (block_size, blocks_per_sm, compact,
+ * use_graph non-zero) are GELIO_ERR_UNSUPPORTED; more than
+ * GELIO_NOALLOC_MAX_SIMS simulations is GELIO_ERR_INVALID_ARGUMENT. */
 #define GELIO_NOALLOC_MAX_SIMS 8
 #define GELIO_NOALLOC_SCRATCH_BYTES 1049344
 int32_t gelio_run_noalloc(const gelio_sim_params *d_sims, int32_t n_sims,

@@ -17,7 +17,10 @@ bool runGpuModel(ParamsCarrier *p, int model) {
     glog::info("Destination is not specified - using generated name for destination: " + destination);
   }
   if (!createDirectory(ghost::modelDirectory(model), destination)) {
+    // as GeliosphereModel.cu:412-416: logged, no simulation, no spectra; the
+    // executable then exits 1 (a run that could not happen)
     glog::error("Directory for the simulation cannot be created.");
+    ghost::runFailed() = true;
     return false;
   }
   gelio_ctx *ctx = ghost::context();

@@ -376,3 +376,18 @@ def test_exit_status_without_a_device(tmp_path):
     assert rc == 255
     rc, err = _exe_run(["-T", "--cpu-only", "-N", "1", "-p", "c"], tmp_path)
     assert rc == 0 and "CPU-only" in err
+
+
+@pytest.mark.parametrize("flag", ["-T", "-E", "-B", "-F"])
+def test_unwritable_results_directory(tmp_path, flag):
+    """A run whose results/<model>/<name> directory cannot be created logs
+    the error and stops before the engine, as the reference does
+    (GeliosphereModel.cu:412-416): no simulation, no log.dat, no spectrum
+    files; the executable exits 1.  The directory is made uncreatable by a
+    regular file named `results` (a permission bit would not stop root)."""
+    (tmp_path / "results").write_text("")
+    rc, err = _exe_run([flag, "-N", "1", "-d", "500"], tmp_path)
+    assert rc == 1
+    assert "Directory for the simulation cannot be created" in err
+    assert "GPU engine unavailable" not in err          # stopped before the engine
+    assert sorted(p.name for p in tmp_path.iterdir()) == ["results"]

@@ -60,7 +60,6 @@ namespace {
 
 struct DeviceSetup {
   bool done = false;
-  int status = GELIO_OK;
   unsigned char *scratch = nullptr;   // device address of g_noalloc_scratch
   int sm_count = 0;
   int occ[3] = {0, 0, 0};             // CTAs of 256 per SM, per kernel variant, model-independent bound
@@ -93,30 +92,30 @@ constexpr unsigned kBlock = 256;
 constexpr size_t kQueueBytes = (kBlock / 32) * (kQueue * sizeof(QEnt) + sizeof(int));
 
 // Once per device, with that device current: resolve the scratch array's
-// device address, fill the bin tables and record the occupancy.  Runs on the first call of gelio_run_noalloc on the
-// device, so that first call should not be made while a stream is being
-// captured.
+// device address, fill the bin tables and record the occupancy.  Runs on the
+// first call of gelio_run_noalloc on the device, so that first call should
+// not be made while a stream is being captured.  The device counts as set up
+// only once every step has succeeded: a failed set-up (e.g. a first call
+// made during a capture, where the table copies are refused) is retried by
+// the next call.  What it records outlives a cudaDeviceReset, which clears
+// the tables: after a reset the process must be restarted before calling
+// gelio_run_noalloc again.
 int setup_device(int dev, DeviceSetup *&out) {
   std::lock_guard<std::mutex> lock(g_setup_mu);
   DeviceSetup &s = g_setup[dev];
   out = &s;
-  if (s.done) return s.status;
-  s.done = true;
+  if (s.done) return GELIO_OK;
   void *ptr = nullptr;
   cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-  if (e != cudaSuccess || ptr == nullptr) { s.status = GELIO_ERR_CUDA; return s.status; }
-  s.scratch = static_cast<unsigned char *>(ptr);
+  if (e != cudaSuccess || ptr == nullptr) return GELIO_ERR_CUDA;
   BinTables t;
   build_tables(t);
   if (fp_tables(t) != cudaSuccess || bp_tables(t) != cudaSuccess || solarprop_tables(t) != cudaSuccess ||
-      geliosphere_tables(t) != cudaSuccess) {
-    s.status = GELIO_ERR_CUDA;
-    return s.status;
-  }
-  if (cudaDeviceGetAttribute(&s.sm_count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
-    s.status = GELIO_ERR_CUDA;
-    return s.status;
-  }
+      geliosphere_tables(t) != cudaSuccess)
+    return GELIO_ERR_CUDA;
+  int sm_count = 0;
+  if (cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return GELIO_ERR_CUDA;
+  int occ_v[2] = {0, 0};
   for (int v = 0; v < 2; ++v) {
     int lowest = 1 << 30;
     for (int m = 0; m < 4; ++m) {
@@ -124,16 +123,18 @@ int setup_device(int dev, DeviceSetup *&out) {
       // in, so no function attribute (shared with gelio_run) is changed
       const void *k = persistent_kernel(m, v);
       int occ = 0;
-      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, (int)kBlock, kQueueBytes) != cudaSuccess || occ < 1) {
-        s.status = GELIO_ERR_UNSUPPORTED;
-        return s.status;
-      }
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, (int)kBlock, kQueueBytes) != cudaSuccess || occ < 1)
+        return GELIO_ERR_UNSUPPORTED;
       if (occ < lowest) lowest = occ;
     }
-    s.occ[v] = lowest;
+    occ_v[v] = lowest;
   }
-  s.status = GELIO_OK;
-  return s.status;
+  s.scratch = static_cast<unsigned char *>(ptr);
+  s.sm_count = sm_count;
+  s.occ[0] = occ_v[0];
+  s.occ[1] = occ_v[1];
+  s.done = true;
+  return GELIO_OK;
 }
 
 }  // namespace
@@ -146,6 +147,11 @@ extern "C" int32_t gelio_run_noalloc(const gelio_sim_params *d_sims, int32_t n_s
   if (n_sims < 0 || n_sims > kMaxN) return GELIO_ERR_INVALID_ARGUMENT;   // beyond the scratch
   if (n_sims > 0 && (d_sims == nullptr || d_out == nullptr)) return GELIO_ERR_INVALID_ARGUMENT;
   if (opts && (opts->plain || opts->record_capacity > 0 || opts->records != nullptr)) return GELIO_ERR_UNSUPPORTED;
+  // the launch shape is fixed (blocks of 256, the occupancy bound per SM,
+  // histograms in the scratch, no graph of its own): asking for another
+  // one is refused rather than ignored
+  if (opts && (opts->block_size != 0 || opts->blocks_per_sm != 0 || opts->compact != 0 || opts->use_graph != 0))
+    return GELIO_ERR_UNSUPPORTED;
   if (opts && opts->precision != GELIO_PREC_FP32 && opts->precision != GELIO_PREC_FP64)
     return GELIO_ERR_INVALID_ARGUMENT;
   if (opts && (opts->refill_interval < 0 || opts->refill_interval % 4 != 0 || opts->refill_interval > 4096 ||

@@ -57,9 +57,20 @@ def argv(args: list[str]):
     return len(args), arr
 
 
-def parse(args: list[str]) -> int:
-    n, arr = argv(["geliosphere", *args])
+def parse(args: list[str], program: str = "geliosphere") -> int:
+    """gelio_host_parse of a command line; `program` is argv[0], whose
+    directory is where month/year runs look for the measured-value tables."""
+    n, arr = argv([program, *args])
     return load().gelio_host_parse(n, arr)
+
+
+def resolve(model: int) -> abi.SimParams:
+    """gelio_sim_params the GPU model would run from the current parameter map."""
+    out = abi.SimParams()
+    st = load().gelio_host_resolve(model, ctypes.byref(out))
+    if st != 0:
+        raise ValueError(f"gelio_host_resolve: status {st}")
+    return out
 
 
 def get_string(key: str, default: str = "") -> str:

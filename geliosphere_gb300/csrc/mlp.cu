@@ -128,6 +128,16 @@ struct gelio_surrogate {
   size_t d_rows_cap = 0, d_rows_used = 0;
   float *d_query = nullptr, *d_yq = nullptr;   // inference inputs / outputs
   size_t query_cap = 0;
+  // predict: simulations and their row offsets on the device, member outputs
+  // [E][stride], ensemble mean / std [2][rows], pinned staging of both ends
+  gelio_sim_params *d_psims = nullptr;
+  long long *d_pfirst = nullptr;
+  size_t psims_cap = 0;
+  float *d_py = nullptr;
+  double *d_pstat = nullptr;
+  size_t prows_cap = 0;
+  unsigned char *h_pstage = nullptr;
+  size_t pstage_cap = 0;
   // inference batches: larger than training batches, so every SM gets
   // several tiles per launch and the resident weights are loaded once per tile
   // group rather than once per tile
@@ -199,6 +209,8 @@ void free_all(gelio_surrogate *s) {
   f(s->yhat); f(s->y); f(s->dy); f(s->partial); f(s->grad); f(s->loss_part); f(s->step_loss);
   f(s->ident); f(s->order); f(s->error); f(s->d_feats); f(s->d_targ); f(s->d_query); f(s->d_yq);
   f(s->Q0); f(s->Q[0]); f(s->Q[1]); f(s->qy); f(s->qident);
+  f(s->d_psims); f(s->d_pfirst); f(s->d_py); f(s->d_pstat);
+  if (s->h_pstage) cudaFreeHost(s->h_pstage);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -629,6 +641,84 @@ int32_t gelio_surrogate_train(gelio_surrogate *s, int32_t epochs, float *last_lo
   return GELIO_OK;
 }
 
+// Ensemble inference of every LOG_GRID point of sims[0..n): the simulations
+// and their row offsets go up (one copy from pinned staging), the features
+// are built on the device per inference batch, every member's layers run on
+// the batch, k_ensemble forms mean and std, and the two come back in one copy.
+int infer_sims(gelio_surrogate *s, const gelio_sim_params *sims, int n, size_t rows, double *ln_ratio,
+               double *ln_std) {
+  const size_t E = s->mem.size();
+  const size_t stride = (rows + kTileM - 1) / kTileM * kTileM;
+  const size_t up = (size_t)n * sizeof(gelio_sim_params) + (size_t)(n + 1) * sizeof(long long);
+  const size_t down = 2 * rows * sizeof(double);
+  if ((size_t)n > s->psims_cap) {
+    if (s->d_psims) cudaFree(s->d_psims);
+    if (s->d_pfirst) cudaFree(s->d_pfirst);
+    s->d_psims = nullptr;
+    s->d_pfirst = nullptr;
+    s->psims_cap = 0;
+    SUR_TRY(gelio::dev_malloc(&s->d_psims, (size_t)n * sizeof(gelio_sim_params)));
+    SUR_TRY(gelio::dev_malloc(&s->d_pfirst, (size_t)(n + 1) * sizeof(long long)));
+    s->psims_cap = (size_t)n;
+  }
+  if (stride > s->prows_cap) {
+    if (s->d_py) cudaFree(s->d_py);
+    if (s->d_pstat) cudaFree(s->d_pstat);
+    s->d_py = nullptr;
+    s->d_pstat = nullptr;
+    s->prows_cap = 0;
+    SUR_TRY(gelio::dev_malloc(&s->d_py, 16 * stride * sizeof(float)));
+    SUR_TRY(gelio::dev_malloc(&s->d_pstat, 2 * stride * sizeof(double)));
+    s->prows_cap = stride;
+  }
+  if (std::max(up, down) > s->pstage_cap) {
+    if (s->h_pstage) cudaFreeHost(s->h_pstage);
+    s->h_pstage = nullptr;
+    s->pstage_cap = 0;
+    SUR_TRY(gelio::pinned_malloc(&s->h_pstage, std::max(up, down)));
+    s->pstage_cap = std::max(up, down);
+  }
+  std::memcpy(s->h_pstage, sims, (size_t)n * sizeof(gelio_sim_params));
+  long long *first = reinterpret_cast<long long *>(s->h_pstage + (size_t)n * sizeof(gelio_sim_params));
+  first[0] = 0;
+  for (int i = 0; i < n; ++i) first[i + 1] = first[i] + sims[i].inj_points;
+  SUR_TRY(cudaEventRecord(s->ev0, s->stream));
+  SUR_TRY(cudaMemcpyAsync(s->d_psims, s->h_pstage, up, cudaMemcpyHostToDevice, s->stream));
+  size_t padded = 0;
+  for (size_t off = 0; off < rows; off += (size_t)s->qrows) {
+    const int c = (int)std::min<size_t>((size_t)s->qrows, rows - off);
+    const int M = (c + kTileM - 1) / kTileM * kTileM;
+    padded += (size_t)M;
+    k_query_features<<<(M + 127) / 128, 128, 0, s->stream>>>(s->d_psims, s->d_pfirst, n, (long long)off, c, M,
+                                                             s->Q0);
+    SUR_TRY(cudaGetLastError());
+    for (size_t e = 0; e < E; ++e) {
+      const int rc = forward_infer_q(s, s->mem[e], M);
+      if (rc != GELIO_OK) return rc;
+      SUR_TRY(cudaMemcpyAsync(s->d_py + e * stride + off, s->qy, (size_t)c * 4, cudaMemcpyDeviceToDevice,
+                              s->stream));
+    }
+  }
+  k_ensemble<<<(unsigned)((rows + 255) / 256), 256, 0, s->stream>>>(s->d_py, (int)E, (long long)rows,
+                                                                    (long long)stride, s->d_pstat,
+                                                                    s->d_pstat + rows);
+  SUR_TRY(cudaGetLastError());
+  SUR_TRY(cudaEventRecord(s->ev1, s->stream));
+  SUR_TRY(cudaMemcpyAsync(s->h_pstage, s->d_pstat, down, cudaMemcpyDeviceToHost, s->stream));
+  const int rc = check_error(s);
+  if (rc != GELIO_OK) return rc;
+  const double *st = reinterpret_cast<const double *>(s->h_pstage);
+  std::memcpy(ln_ratio, st, rows * sizeof(double));
+  if (ln_std) std::memcpy(ln_std, st + rows, rows * sizeof(double));
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, s->ev0, s->ev1) == cudaSuccess) {
+    s->last_ms = ms;
+    s->last_flop = 2.0 * (double)padded * (double)E *
+                   ((double)kInPad * kWidth + 3.0 * kWidth * kWidth + (double)kWidth);
+  }
+  return GELIO_OK;
+}
+
 int32_t gelio_surrogate_forward(gelio_surrogate *s, int32_t member, const float *x, int32_t n, float *y) {
   if (!valid_member(s, member) || n < 0 || (n > 0 && (!x || !y))) return GELIO_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lock(s->mu);
@@ -705,39 +795,17 @@ int32_t gelio_surrogate_predict(gelio_surrogate *s, const gelio_sim_params *sims
   if (!s || n < 0 || (n > 0 && (!sims || !ln_ratio))) return GELIO_ERR_INVALID_ARGUMENT;
   for (auto &m : s->mem)
     if (!m.trained) return GELIO_ERR_NOT_TRAINED;
-  std::vector<float> x;
   size_t rows = 0;
   for (int i = 0; i < n; ++i) {
-    if (sims[i].injection != GELIO_INJ_LOG_GRID || sims[i].inj_points < 1 || sims[i].inj_points > GELIO_GRID_MAX)
+    if (sims[i].injection != GELIO_INJ_LOG_GRID || sims[i].inj_points < 1 || sims[i].inj_points > GELIO_GRID_MAX ||
+        !(sims[i].inj_min > 0.f) || !(sims[i].inj_max > 0.f))
       return GELIO_ERR_INVALID_ARGUMENT;
-    for (int j = 0; j < sims[i].inj_points; ++j) {
-      float f[kFeatures];
-      gelio_surrogate_features(&sims[i], grid_energy(sims[i], j), f);
-      x.insert(x.end(), f, f + kFeatures);
-      ++rows;
-    }
+    rows += (size_t)sims[i].inj_points;
   }
   if (rows == 0) return GELIO_OK;
-  const int E = (int)s->mem.size();
-  std::vector<float> y((size_t)E * rows);
-  {
-    std::lock_guard<std::mutex> lock(s->mu);
-    SUR_TRY(cudaSetDevice(s->device));
-    const int rc = infer_rows(s, 0, E, x.data(), rows, y.data());
-    if (rc != GELIO_OK) return rc;
-  }
-  for (size_t r = 0; r < rows; ++r) {
-    double mu = 0.0, m2 = 0.0;
-    for (int e = 0; e < E; ++e) mu += y[(size_t)e * rows + r];
-    mu /= E;
-    for (int e = 0; e < E; ++e) {
-      const double d = y[(size_t)e * rows + r] - mu;
-      m2 += d * d;
-    }
-    ln_ratio[r] = mu;
-    if (ln_std) ln_std[r] = E > 1 ? std::sqrt(m2 / (E - 1)) : 0.0;
-  }
-  return GELIO_OK;
+  std::lock_guard<std::mutex> lock(s->mu);
+  SUR_TRY(cudaSetDevice(s->device));
+  return infer_sims(s, sims, n, rows, ln_ratio, ln_std);
 }
 
 int32_t gelio_surrogate_spectra(gelio_surrogate *s, const gelio_sim_params *sims, int32_t n,

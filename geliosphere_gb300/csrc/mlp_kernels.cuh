@@ -15,6 +15,7 @@
 #pragma once
 #include <cuda_bf16.h>
 
+#include "gelio.h"
 #include "tc_sm103.cuh"
 
 namespace gelio {
@@ -481,6 +482,67 @@ __global__ void k_pack(const float *__restrict__ p, __nv_bfloat16 *__restrict__ 
     w3t[i * kWidth + o] = b;
     w4t[i * kWidth + o] = c;
   }
+}
+
+// ---------------------------------------------------------------------------
+// Inference queries built on the device (gelio_surrogate_predict).
+// ---------------------------------------------------------------------------
+
+// Network input of grid point j of simulation s: the LOG_GRID energy as the
+// SDE kernels build it (FP64 log / exp, rounded to FP32) and the
+// normalisation of gelio_surrogate_features, evaluated in FP64 and rounded
+// to FP32 like the host function.
+__device__ __forceinline__ void query_features(const gelio_sim_params &s, int j, float f[kFeatures]) {
+  const double lmin = log((double)s.inj_min), lmax = log((double)s.inj_max);
+  const double fr = (s.inj_points > 1) ? (double)j / (double)(s.inj_points - 1) : 0.0;
+  const float T = (float)exp(lmin + fr * (lmax - lmin));
+  const double rad = 180.0 / 3.14159265358979323846;
+  f[0] = (float)((log10((double)s.K0 / 4.4683705e-27) - 22.5) * 2.0);
+  f[1] = (float)(((double)s.V / 6.68458712e-9 - 550.0) / 200.0);
+  f[2] = (float)(((double)s.tilt * rad - 40.0) / 35.0);
+  f[3] = (float)s.polarity;
+  f[4] = (float)(((double)s.r_injection - 40.5) / 39.5);
+  f[5] = (float)(((double)s.theta_injection * rad - 90.0) / 80.0);
+  f[6] = (float)(log10((double)T) / 2.0);
+}
+
+// Rows [off, off + c) of the query (row = first[i] + j: grid point j of
+// simulation i) into the BF16 first-layer operand x0 [M][kInPad]; rows c..M-1
+// of the tile padding are zero.
+__global__ void k_query_features(const gelio_sim_params *__restrict__ sims, const long long *__restrict__ first,
+                                 int n_sims, long long off, int c, int M, __nv_bfloat16 *__restrict__ x0) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= M) return;
+  float f[kFeatures] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (m < c) {
+    const long long row = off + m;
+    int lo = 0, hi = n_sims - 1;          // last simulation with first[i] <= row
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (first[mid] <= row) lo = mid; else hi = mid - 1;
+    }
+    query_features(sims[lo], (int)(row - first[lo]), f);
+  }
+#pragma unroll
+  for (int k = 0; k < kFeatures; ++k) x0[(size_t)m * kInPad + k] = __float2bfloat16_rn(f[k]);
+}
+
+// Ensemble mean and sample standard deviation (FP64) of E member outputs
+// y[e * stride + row].
+__global__ void k_ensemble(const float *__restrict__ y, int E, long long rows, long long stride,
+                           double *__restrict__ mean, double *__restrict__ sd) {
+  const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rows) return;
+  double mu = 0.0;
+  for (int e = 0; e < E; ++e) mu += (double)y[(size_t)e * stride + r];
+  mu /= E;
+  double m2 = 0.0;
+  for (int e = 0; e < E; ++e) {
+    const double d = (double)y[(size_t)e * stride + r] - mu;
+    m2 += d * d;
+  }
+  mean[r] = mu;
+  sd[r] = (E > 1) ? sqrt(m2 / (E - 1)) : 0.0;
 }
 
 }  // namespace mlp

@@ -155,3 +155,34 @@ def test_training_is_deterministic_and_params_round_trip(engine):
     s.set_params(1, ps[0])
     np.testing.assert_array_equal(s.get_params(1), ps[0])
     s.close()
+
+
+def test_predict_builds_queries_on_the_device(engine):
+    """gelio_surrogate_predict builds each grid point's network input on the
+    device: its ensemble mean and std equal those of the members run one by
+    one (gelio_surrogate_forward) on the host-built inputs of
+    gelio_surrogate_features, over ragged grids and more rows than one
+    inference batch."""
+    s = sg.Surrogate(engine, members=3, batch_rows=1024, seed=9)
+    try:
+        for m in range(3):
+            s.set_params(m, init_params(seed=40 + m))
+        rng = np.random.default_rng(8)
+        sims = []
+        for i in range(700):
+            pts = int(rng.integers(1, 200))
+            sims.append(make_sim(abi.GELIO_MODEL_2D_GELIOSPHERE, 1, K0_cm2s=float(rng.uniform(1e22, 1e23)),
+                                 V_kms=float(rng.uniform(350, 750)), tilt_deg=float(rng.uniform(5, 75)),
+                                 polarity=int(rng.choice([-1, 1])), r_injection=float(rng.uniform(1, 80)),
+                                 theta_deg=float(rng.uniform(10, 170)), injection=abi.GELIO_INJ_LOG_GRID,
+                                 inj_min=float(rng.uniform(0.005, 0.05)), inj_max=float(rng.uniform(50, 200)),
+                                 inj_points=pts))
+        rows = sum(x.inj_points for x in sims)
+        assert rows > 65_536
+        mean, sd = s.predict(sims)
+        x = np.stack([s.features(sim, sg.grid_energies(sim)[j]) for sim in sims for j in range(sim.inj_points)])
+        y = np.stack([s.forward(m, x).astype(np.float64) for m in range(3)])
+        np.testing.assert_allclose(np.concatenate(mean), y.mean(axis=0), rtol=1e-12, atol=1e-12)
+        np.testing.assert_allclose(np.concatenate(sd), y.std(axis=0, ddof=1), rtol=1e-9, atol=1e-12)
+    finally:
+        s.close()

@@ -311,12 +311,12 @@ void build_tables(BinTables &t) {
   memcpy(t.sp, sp, sizeof(t.sp));
   memcpy(t.uly, uly, sizeof(t.uly));
   memcpy(t.ams, ams, sizeof(t.ams));
-  // OneDimensionBpResults.cpp:158-165 with NT = 80, Tmin = 0.01, Tmax = 200.
+  // OneDimensionBpResults.cpp:25-31 with NT = 80, Tmin = 0.01, Tmax = 200.
   const double dlT = log10(200.0 / 0.01) / 80;
   const double X = log10(200.0);
   for (int i = 0; i < 80; i++) t.bp_log[i] = exp((X - (i * dlT)) * log(10.0));
   t.bp_log[80] = 0.0;
-  // OneDimensionFpResults.cpp:269-272.
+  // OneDimensionFpResults.cpp:24-27.
   for (int i = 0; i < 25; i++) t.fp_log[i] = exp((((i + 1) / 5.0) - 3.0) * log(10));
   // getSolarPropInjection energies 0.01 * 1.5^k, rounded once to FP32.
   for (int k = 0; k < 30; ++k) t.sp30[k] = (float)(0.01 * pow(1.5, k));
@@ -1014,6 +1014,8 @@ int32_t gelio_autotune(gelio_ctx *c, const gelio_sim_params *sims, int32_t n, ge
     t.refill = bo.refill_interval;
     t.compact = bo.compact;
     t.blocks_per_sm = 0;
+    // a cached graph was captured with the shapes chosen before
+    if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
   }
   if (best) *best = bo;
   return GELIO_OK;

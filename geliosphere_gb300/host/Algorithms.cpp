@@ -266,6 +266,37 @@ int batchPlan(ParamsCarrier *p, const std::string &path, std::vector<gelio_sim_p
   return (int)plan.size();
 }
 
+// Launch shapes of a large batch picked by gelio_autotune: for each model
+// in the batch, its rows with their particle counts scaled down (the sample
+// holds about total / 256 particles, between 1 and 4 million, at least 4096
+// per row) are timed over the tuner's block sizes, refill intervals and
+// exit-queue modes, and the winner is kept in the context for that model.
+// Batches below 2e7 particles run in the default shapes (tuning would cost
+// more than it could save).
+static void tuneBatch(gelio_ctx *ctx, const std::vector<gelio_sim_params> &sims) {
+  for (int m = 0; m < 4; ++m) {
+    std::vector<gelio_sim_params> rows;
+    int64_t total = 0;
+    for (const auto &s : sims)
+      if (s.model == m && s.n_particles > 0) {
+        rows.push_back(s);
+        total += s.n_particles;
+      }
+    if (rows.empty() || total < 20000000) continue;
+    const double target = std::min(4.0e6, std::max(1.0e6, (double)total / 256.0));
+    const double scale = target / (double)total;
+    for (auto &r : rows) r.n_particles = std::max<int64_t>(4096, (int64_t)((double)r.n_particles * scale));
+    gelio_run_opts best = {};
+    const int st = gelio_autotune(ctx, rows.data(), (int32_t)rows.size(), &best);
+    if (st != GELIO_OK)
+      glog::warn(std::string("Autotuning skipped: ") + gelio_status_string(st));
+    else
+      glog::info("Tuned launch for model " + std::to_string(m) + ": block " + std::to_string(best.block_size) +
+                 ", refill every " + std::to_string(best.refill_interval) + " steps, exit queue mode " +
+                 std::to_string(best.compact) + ".");
+  }
+}
+
 // Every row that resolves is added to one gelio_run call, so all
 // simulations of the batch share one persistent launch per model.  Each
 // row's directory then receives its spectra and, when kept, its log.dat.
@@ -288,6 +319,10 @@ void BatchRun::runAlgorithm(ParamsCarrier *p) {
   }
   std::vector<gelio_exit_record> recs;
   gelio_run_opts opts = {};
+  tuneBatch(ctx, sims);
+  // the whole batch is one graph-captured sequence (upload, prepare, one
+  // persistent launch per model, reduce, download) in the tuned shapes
+  opts.use_graph = 1;
   if (anyLog) {
     recs.resize((size_t)cap);
     opts.records = recs.data();

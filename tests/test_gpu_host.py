@@ -148,6 +148,31 @@ def test_batch_one_launch_equals_single_runs(exe, tmp_path):
             same_table(got / f, ref / f, f)
 
 
+def test_large_batch_is_autotuned_and_equals_single_runs(exe, tmp_path):
+    """A batch of 2e7 2D Geliosphere particles is tuned (gelio_autotune on a
+    scaled-down copy of its rows) and run as one graph-captured launch; the
+    tuned shape changes no spectrum (each particle keeps its own random
+    stream), so every row equals the same row run alone."""
+    s = settings(tmp_path)
+    rows = [("g1", "2D Geliosphere", "10"), ("g2", "2D Geliosphere", "10"), ("sp", "2D SolarProp-like", "1")]
+    csv = tmp_path / "batch.csv"
+    csv.write_text("name,month,year,V,K0,dt,r,theta,N,model,pathToCustomSettingsFile\n" +
+                   "".join(f"{n},,,,,,,,{N},{m},{s}\n" for n, m, N in rows))
+    rc, err = run(exe, ["-b", str(csv)], tmp_path, seed=11)
+    assert rc == 0, err
+    assert "Tuned launch for model 3" in err and "Tuned launch for model 2" not in err
+    dirs = {"2D Geliosphere": ("Geliosphere2D", "-T"), "2D SolarProp-like": ("SOLARPROPLike", "-E")}
+    for i, (name, model, N) in enumerate(rows, start=1):
+        d, flag = dirs[model]
+        single = tmp_path / f"single_{i}"
+        single.mkdir()
+        seed = (11 + i * 0x9E3779B97F4A7C15) % (1 << 64)
+        rc, err = run(exe, [flag, "-N", N, "-p", "s", "-s", s], single, seed=seed)
+        assert rc == 0, err
+        for f in SPECTRA_2D:
+            same_table(tmp_path / "results" / d / name / f, single / "results" / d / "s" / f, f)
+
+
 @pytest.mark.parametrize("flag,d,files", [("-T", "eval_2d", SPECTRA_2D), ("-B", "eval_bp", SPECTRA_1D),
                                           ("-F", "eval_fp", SPECTRA_1D)])
 def test_cli_evaluation_reproduces_reference_evaluator_files(exe, tmp_path, flag, d, files):

@@ -2,8 +2,8 @@
 // and binnings, applied to each exit record as it happens.
 //
 //   2D    Algorithm/src/TwoDimensionBpResults.cpp:40-105
-//   1D B-p Algorithm/src/OneDimensionBpResults.cpp:158-220
-//   1D F-p Algorithm/src/OneDimensionFpResults.cpp:269-333
+//   1D B-p Algorithm/src/OneDimensionBpResults.cpp:20-87
+//   1D F-p Algorithm/src/OneDimensionFpResults.cpp:19-88
 //   constants Algorithm/include/ResultConstants.hpp:19-117
 //
 // In the reference the simulation prints each record to log.dat with "%g"
@@ -76,8 +76,8 @@ struct BinTables {
   double sp[32];        // SPbins (ResultConstants.hpp:86-90)
   double uly[4];        // UlyssesBins
   double ams[72];       // AmsBins
-  double bp_log[81];    // binb[i] = 10^(X - i dlT), i < NT = 80 (OneDimensionBpResults.cpp:158-165)
-  double fp_log[25];    // binb[i] = 10^((i+1)/5 - 3)          (OneDimensionFpResults.cpp:269-272)
+  double bp_log[81];    // binb[i] = 10^(X - i dlT), i < NT = 80 (OneDimensionBpResults.cpp:25-31)
+  double fp_log[25];    // binb[i] = 10^((i+1)/5 - 3)          (OneDimensionFpResults.cpp:24-27)
   float sp30[30];       // getSolarPropInjection energies 0.01 * 1.5^k
 };
 
@@ -152,14 +152,14 @@ __device__ __forceinline__ double lis_burger(double T) {
   return j / (1 + tem);
 }
 
-// Yamada et al. 1998 weight of OneDimensionBpResults.cpp:191-193 (no 1e45
-// scaling) and of OneDimensionFpResults.cpp:300-302 (scaled by 1e-45).
+// Yamada et al. 1998 weight of OneDimensionBpResults.cpp:58-60 (no 1e45
+// scaling) and of OneDimensionFpResults.cpp:56-57 (scaled by 1e-45).
 __device__ __forceinline__ double yamada(double p) {
   const double w = (kM0 * kM0 * kC * kC * kC * kC) + (p * p * kC * kC);
   return exp(-1.85 * log(w)) / p;
 }
 
-// Kinetic energy [GeV] from an SI momentum, as OneDimensionFpResults.cpp:297-299.
+// Kinetic energy [GeV] from an SI momentum, as OneDimensionFpResults.cpp:51-54.
 __device__ __forceinline__ double fp_tkin_from_p(double p1AU) {
   const double T0 = kM0 * kC * kC / (kQ * 1e9);
   const double Rig = p1AU * kC / kQ;

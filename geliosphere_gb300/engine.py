@@ -218,7 +218,7 @@ class Engine:
 
 # ---------------------------------------------------------------------------
 # log.dat rows of exit records, as the reference's writers print them
-# (GeliosphereModel.cu:442, OneDimensionBpModel.cu:497, OneDimensionFpModel.cu:195)
+# (GeliosphereModel.cu:442, OneDimensionBpModel.cu:192, OneDimensionFpModel.cu:195)
 # ---------------------------------------------------------------------------
 _Q, _C, _M0 = 1.60219e-19, 2.99793e8, 1.67261e-27
 _T0W = _M0 * _C * _C

@@ -34,7 +34,7 @@ bool &runFailed();
 gelio_sim_params resolveSimParams(ParamsCarrier *p, int model);
 
 // Reference log.dat line of one exit record (the GPU writers,
-// GeliosphereModel.cu:442, OneDimensionBpModel.cu:497, OneDimensionFpModel.cu:195).
+// GeliosphereModel.cu:442, OneDimensionBpModel.cu:192, OneDimensionFpModel.cu:195).
 std::string logLine(int model, const gelio_exit_record &r, float thetaInjection);
 
 int modelFromName(const std::string &name);   // -1 if unknown

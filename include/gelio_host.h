@@ -73,7 +73,7 @@ int32_t gelio_host_batch_plan(const char *csv_path, gelio_sim_params *out, int32
 int32_t gelio_host_write_spectra(int32_t model, const gelio_spectra *s, int32_t csv, const char *dir);
 
 /* One log.dat line of an exit record as the GPU models print it
- * (GeliosphereModel.cu:442, OneDimensionBpModel.cu:497, OneDimensionFpModel.cu:195);
+ * (GeliosphereModel.cu:442, OneDimensionBpModel.cu:192, OneDimensionFpModel.cu:195);
  * returns the length, copies at most cap-1 bytes. */
 int32_t gelio_host_log_line(int32_t model, const gelio_exit_record *r, float theta_injection, char *buf,
                             int32_t cap);

@@ -14,7 +14,7 @@
 //   Seeded like the reference, it reproduces the reference CPU models'
 //   output records, which pins this restatement to the reference itself:
 //     GeliosphereCpuModel.cpp:55-409, SolarPropLikeCpuModel.cpp:55-258,
-//     OneDimensionBpCpuModel.cpp:54-143, OneDimensionFpCpuModel.cpp:196-298.
+//     OneDimensionBpCpuModel.cpp:54-143, OneDimensionFpCpuModel.cpp:53-155.
 //
 // * "gpu" flavour: the reference GPU kernels' semantics in FP64, with the
 //   FP32 constant values of CosmicConstants.cu:14-41, driven by the engine's
@@ -26,7 +26,7 @@
 //     CosmicUtils.cu:17-40.
 //
 // * evaluators: TwoDimensionBpResults.cpp:13-106, OneDimensionBpResults.cpp:
-//   13-220, OneDimensionFpResults.cpp:13-333 on parsed log.dat rows.
+//   13-112, OneDimensionFpResults.cpp:13-113 on parsed log.dat rows.
 //
 // Parity anchor: the reference has no tests or golden vectors; the "cpu"
 // flavour is pinned against the reference CPU models and evaluators
@@ -377,7 +377,7 @@ void gpu_solarprop(const gelio_sim_params &p, uint64_t pid, uint64_t max_steps, 
 }
 
 // Kinetic energy [GeV] from momentum, as the GPU kernels' Eq. 6 "in J"
-// (OneDimensionBpModel.cu:418-419) with p expressed as rigidity P [GV]:
+// (OneDimensionBpModel.cu:114) with p expressed as rigidity P [GV]:
 // T = (sqrt(T0^2 q^2 1e18 + q^2 Rig^2) - T0 q 1e9) / (q 1e9), Rig = P 1e9.
 double tkin_from_P(double P, double T0) {
   const double q = 1.60219e-19;

@@ -570,9 +570,11 @@ def run_surrogate(args, eng, rank, world, local):
             "e2e": {"value": sur_rate, "unit": "spectra/s",
                     "h2d_bytes_per_step": len(test) * 100 * 7 * 4,
                     "d2h_bytes_per_step": len(test) * 100 * 5 * 4},
-            "gpu_launches": -(-len(test) * 100 // 8192) * (1 + 5 * 4),
+            # per 65,536-row inference batch: the query features and the fused
+            # network (every member); then the ensemble statistics
+            "gpu_launches": 2 * -(-len(test) * 100 // 65536) + 1,
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
-                         "frac": achieved / bf16_peak, "traffic": None, "kernel": "k_mlp_gemm<INFER*> (tcgen05)",
+                         "frac": achieved / bf16_peak, "traffic": None, "kernel": "k_mlp_infer_fused (tcgen05, all layers and members in one launch)",
                          "device_ms": dev_ms, "flop": flop,
                          "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if peaks else
                                         "fallback 1.9 PFLOP/s bf16 burst"}}

@@ -192,6 +192,9 @@ int set_smem_attrs() {
     set((const void *)k_mlp_gemm<INFER_LAST>);
     set((const void *)k_mlp_gemm<DX>);
     set((const void *)k_mlp_gemm<DW>);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute((const void *)k_mlp_infer_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)kFusedSmem);
     rc = cuda_status(e);
   });
   return rc;
@@ -641,6 +644,33 @@ int32_t gelio_surrogate_train(gelio_surrogate *s, int32_t epochs, float *last_lo
   return GELIO_OK;
 }
 
+// Every member on the first c rows of the inference batch (s->Q0, zero past
+// c up to a whole tile) in one launch of the fused network kernel; member e's
+// outputs go to y[e * stride + row].
+int infer_fused(gelio_surrogate *s, int c, float *y, long long stride) {
+  const int E = (int)s->mem.size();
+  if (E > kFusedMaxMembers) return GELIO_ERR_UNSUPPORTED;
+  FusedMaps maps;
+  maps.q0 = s->mQ0;
+  FusedArgs a{};
+  for (int e = 0; e < E; ++e) {
+    maps.w[e][0] = s->mem[e].mW1;
+    for (int l = 0; l < 3; ++l) maps.w[e][l + 1] = s->mem[e].mW[l];
+    a.P[e] = s->mem[e].P;
+  }
+  a.M = c;
+  a.n_pairs = (c + 2 * kTileM - 1) / (2 * kTileM);
+  a.E = E;
+  a.stride = stride;
+  a.y = y;
+  a.error = s->error;
+  a.timeout_ns = 2000000000ull;
+  const int items = E * a.n_pairs;
+  const int grid = std::max(1, std::min(items, s->sm_count));
+  k_mlp_infer_fused<<<grid, kGemmThreads, kFusedSmem, s->stream>>>(maps, a);
+  return cuda_status(cudaGetLastError());
+}
+
 // Ensemble inference of every LOG_GRID point of sims[0..n): the simulations
 // and their row offsets go up (one copy from pinned staging), the features
 // are built on the device per inference batch, every member's layers run on
@@ -688,16 +718,12 @@ int infer_sims(gelio_surrogate *s, const gelio_sim_params *sims, int n, size_t r
   for (size_t off = 0; off < rows; off += (size_t)s->qrows) {
     const int c = (int)std::min<size_t>((size_t)s->qrows, rows - off);
     const int M = (c + kTileM - 1) / kTileM * kTileM;
-    padded += (size_t)M;
+    padded += (size_t)(c + 2 * kTileM - 1) / (2 * kTileM) * (2 * kTileM);   // rows the fused kernel multiplies
     k_query_features<<<(M + 127) / 128, 128, 0, s->stream>>>(s->d_psims, s->d_pfirst, n, (long long)off, c, M,
                                                              s->Q0);
     SUR_TRY(cudaGetLastError());
-    for (size_t e = 0; e < E; ++e) {
-      const int rc = forward_infer_q(s, s->mem[e], M);
-      if (rc != GELIO_OK) return rc;
-      SUR_TRY(cudaMemcpyAsync(s->d_py + e * stride + off, s->qy, (size_t)c * 4, cudaMemcpyDeviceToDevice,
-                              s->stream));
-    }
+    const int rc = infer_fused(s, c, s->d_py + off, (long long)stride);
+    if (rc != GELIO_OK) return rc;
   }
   k_ensemble<<<(unsigned)((rows + 255) / 256), 256, 0, s->stream>>>(s->d_py, (int)E, (long long)rows,
                                                                     (long long)stride, s->d_pstat,

@@ -352,6 +352,240 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
 }
 
 // ----------------------------------------------------------------------------
+// Whole-network inference, all ensemble members in one persistent launch.
+//
+// Work item = (member e, 256 query rows): two 128-row tiles run the four
+// hidden layers in lockstep and share every weight chunk.  The activations
+// never leave the SM: each layer's epilogue writes bias + SiLU as BF16
+// straight into shared memory in the K-major 128-byte-swizzle layout that
+// the next layer's tcgen05.mma reads (the layout TMA would write), and the
+// last layer's epilogue forms the 256 -> 1 head.  Only the first layer's
+// input (the query features, TMA) and the weights (32 KiB K-chunks of
+// [256 N][64 K], TMA from L2, a 2-stage ring) are loaded.
+//   warp 0 (one lane)  TMA: the item's two input tiles, then 13 weight chunks
+//   warp 1 (one lane)  MMA: per layer and K-chunk one N = 256 product per tile
+//                      into that tile's TMEM accumulator (2 x 256 columns)
+//   warps 2-9          epilogue: warp w takes TMEM lane quarter w % 4 of
+//                      tile (w - 2) / 4, all 256 columns of its 32 rows
+// Every value equals the layer-by-layer INFER / INFER_LAST path bit for bit:
+// the same operands in the same K order, the same epilogue arithmetic and
+// the head summed as (sum of columns 0-127 + b5) + sum of columns 128-255.
+// Shared memory: A (2 x 64 KiB) + weight ring (2 x 32 KiB) + biases.
+// ----------------------------------------------------------------------------
+constexpr int kFusedMaxMembers = 16;
+constexpr int kFusedStages = 2;
+constexpr uint32_t kFusedA = kTileM * kWidth * 2;                 // 64 KiB: one tile's activations
+constexpr size_t kFusedSmem = 1024 + 2 * (size_t)kFusedA + kFusedStages * (size_t)kStageB + 256;
+
+struct FusedMaps {
+  CUtensorMap q0;                                  // queries [rows][64], box {64, 128}
+  CUtensorMap w[kFusedMaxMembers][4];              // W1 [256][64], W2-W4 [256][256], box {64, 256}
+};
+
+struct FusedArgs {
+  int M;                        // query rows
+  int n_pairs;                  // ceil(M / 256)
+  int E;                        // members
+  long long stride;             // y row stride per member
+  const float *P[kFusedMaxMembers];   // FP32 parameters of each member (biases, head)
+  float *y;                     // [E][stride] head outputs
+  unsigned *error;
+  unsigned long long timeout_ns;
+};
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void named_sync(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+__global__ void __launch_bounds__(kGemmThreads, 1)
+    k_mlp_infer_fused(const __grid_constant__ FusedMaps maps, const FusedArgs a) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ float s_b[4][kWidth], s_w5[kWidth];
+  const uint32_t s0 = tc::smem_u32(smem_raw);
+  unsigned char *base = smem_raw + ((1024u - (s0 & 1023u)) & 1023u);
+  unsigned char *ring = base + 2 * kFusedA;          // A of tile t: base + t * kFusedA
+  uint64_t *full = reinterpret_cast<uint64_t *>(ring + kFusedStages * kStageB);
+  uint64_t *empty = full + kFusedStages;
+  uint64_t *a_full = empty + kFusedStages;      // the item's input tiles landed
+  uint64_t *a_empty = a_full + 1;               // the item's last products read A
+  uint64_t *acc_full = a_empty + 1;             // a layer's products are in TMEM
+  uint64_t *acc_empty = acc_full + 1;           // a layer's epilogue read TMEM and wrote A
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(acc_empty + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int items = a.E * a.n_pairs;
+  if (tid == 0) {
+    for (int st = 0; st < kFusedStages; ++st) {
+      tc::mbar_init(&full[st], 1);
+      tc::mbar_init(&empty[st], 1);
+    }
+    tc::mbar_init(a_full, 1);
+    tc::mbar_init(a_empty, 1);
+    tc::mbar_init(acc_full, 1);
+    tc::mbar_init(acc_empty, kEpiWarps);
+    tc::fence_mbar_init();
+    tc::tma_prefetch(&maps.q0);
+  }
+  if (warp == 1) {
+    tc::tmem_alloc(tslot, 2 * kTmemCols);
+    tc::tmem_relinquish();
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = *tslot;
+  const unsigned long long deadline = tc::now_ns() + a.timeout_ns;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      uint32_t it = 0, local = 0, a_loads = 0;
+      bool ok = true;
+      for (int w = blockIdx.x; w < items && ok; w += gridDim.x, ++local) {
+        const int e = w / a.n_pairs, pair = w % a.n_pairs;
+        // the previous item's last products have read A
+        if (local > 0 && !tc::mbar_wait(a_empty, (local - 1) & 1, deadline)) { ok = false; break; }
+        ++a_loads;
+        tc::mbar_expect_tx(a_full, 2 * kStageA);
+        tc::tma_load_2d(base, &maps.q0, 0, pair * 2 * kTileM, a_full);
+        tc::tma_load_2d(base + kFusedA, &maps.q0, 0, pair * 2 * kTileM + kTileM, a_full);
+        for (int l = 0; l < 4 && ok; ++l) {
+          const int nk = (l == 0) ? 1 : kWidth / kChunk;
+          for (int kc = 0; kc < nk; ++kc) {
+            const uint32_t st = it % kFusedStages;
+            if (it >= (uint32_t)kFusedStages &&
+                !tc::mbar_wait(&empty[st], ((it / kFusedStages) - 1) & 1, deadline)) {
+              ok = false;
+              break;
+            }
+            tc::mbar_expect_tx(&full[st], kStageB);
+            tc::tma_load_2d(ring + st * kStageB, &maps.w[e][l], kc * kChunk, 0, &full[st]);
+            ++it;
+          }
+        }
+      }
+      if (!ok) {
+        atomicExch(a.error, 11u);
+        // copies in flight land before the shared memory is given back
+        const unsigned long long d2 = tc::now_ns() + 1000000000ull;
+        for (uint32_t j = (it > (uint32_t)kFusedStages ? it - kFusedStages : 0u); j < it; ++j)
+          tc::mbar_wait(&full[j % kFusedStages], (j / kFusedStages) & 1, d2);
+        if (a_loads > 0) tc::mbar_wait(a_full, (a_loads - 1) & 1, d2);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = tc::idesc_bf16_f32(kTileM, kWidth);
+      uint32_t it = 0, layer = 0, local = 0;
+      bool ok = true;
+      for (int w = blockIdx.x; w < items && ok; w += gridDim.x, ++local) {
+        if (!tc::mbar_wait(a_full, local & 1, deadline)) { ok = false; break; }
+        for (int l = 0; l < 4 && ok; ++l, ++layer) {
+          // the previous layer's epilogue has read TMEM and written A
+          if (layer > 0 && !tc::mbar_wait(acc_empty, (layer - 1) & 1, deadline)) { ok = false; break; }
+          tc::tc_fence_after();
+          const int nk = (l == 0) ? 1 : kWidth / kChunk;
+          for (int kc = 0; kc < nk; ++kc) {
+            const uint32_t st = it % kFusedStages;
+            if (!tc::mbar_wait(&full[st], (it / kFusedStages) & 1, deadline)) { ok = false; break; }
+            tc::tc_fence_after();
+            const uint32_t bb = tc::smem_u32(ring + st * kStageB);
+#pragma unroll
+            for (int t = 0; t < 2; ++t) {
+              const uint32_t aa = tc::smem_u32(base + t * kFusedA + kc * kStageA);
+#pragma unroll
+              for (int k = 0; k < kChunk / 16; ++k)
+                tc::mma_bf16(tmem + (uint32_t)t * kTmemCols, tc::sdesc_sw128(aa + k * 32),
+                             tc::sdesc_sw128(bb + k * 32), idesc, (kc > 0 || k > 0) ? 1u : 0u);
+            }
+            tc::mma_commit(&empty[st]);
+            ++it;
+          }
+          if (!ok) break;
+          tc::mma_commit(acc_full);
+          if (l == 3) tc::mma_commit(a_empty);
+        }
+      }
+      if (!ok) {
+        atomicExch(a.error, 12u);
+        // products in flight finish before TMEM is given back
+        const unsigned long long d2 = tc::now_ns() + 1000000000ull;
+        if (it > 0) tc::mbar_wait(&empty[(it - 1) % kFusedStages], ((it - 1) / kFusedStages) & 1, d2);
+      }
+    }
+  } else {
+    const int q = warp & 3;                        // TMEM lane quarter
+    const int t = (warp - 2) >> 2;                 // tile of the pair
+    const int r = q * 32 + lane;                   // row in the tile
+    const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)t * kTmemCols;
+    unsigned char *arow = base + t * kFusedA + r * 128;
+    uint32_t layer = 0;
+    bool ok = true;
+    // A warp whose wait ran out keeps walking the items without waiting or
+    // working, so every epilogue warp reaches the same named barriers.
+    for (int w = blockIdx.x; w < items; w += gridDim.x) {
+      const int e = w / a.n_pairs, pair = w % a.n_pairs;
+      // this member's biases and head (every epilogue warp is past the
+      // previous item before they are replaced)
+      named_sync(1, 32 * kEpiWarps);
+      const float *P = a.P[e];
+      for (int i = tid - 64; i < kWidth; i += 32 * kEpiWarps) {
+        s_b[0][i] = P[kOffB1 + i];
+        s_b[1][i] = P[kOffB2 + i];
+        s_b[2][i] = P[kOffB3 + i];
+        s_b[3][i] = P[kOffB4 + i];
+        s_w5[i] = P[kOffW5 + i];
+      }
+      named_sync(1, 32 * kEpiWarps);
+      for (int l = 0; l < 4; ++l, ++layer) {
+        if (ok) ok = __all_sync(0xffffffffu, tc::mbar_wait(acc_full, layer & 1, deadline));
+        if (!ok) continue;
+        tc::tc_fence_after();
+        float h0 = 0.0f, hs = 0.0f;            // head: columns 0-127, then the running half
+        for (int c = 0; c < kWidth / 32; ++c) {
+          if (c == 4) { h0 = hs; hs = 0.0f; }
+          float v[32];
+          tc::tmem_ld32(trow + (uint32_t)(c * 32), v);
+          __align__(16) __nv_bfloat16 out[32];
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const float z = v[j] + s_b[l][c * 32 + j];
+            out[j] = __float2bfloat16_rn(silu_f(z));
+            if (l == 3) hs += __bfloat162float(out[j]) * s_w5[c * 32 + j];
+          }
+          if (l < 3) {
+            // columns 32c .. 32c+31 = K-chunk c / 2, 16-byte pieces 4 (c % 2) .. +3
+            const uint4 *src = reinterpret_cast<const uint4 *>(out);
+            unsigned char *chunk = arow + (c >> 1) * kStageA;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+              const int piece = ((c & 1) * 4 + i) ^ (r & 7);
+              *reinterpret_cast<uint4 *>(chunk + piece * 16) = src[i];
+            }
+          }
+        }
+        if (l < 3) fence_proxy_async_smem();     // A written for the tensor core
+        tc::tc_fence_before();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(acc_empty);
+        if (l == 3) {
+          const int row = pair * 2 * kTileM + t * kTileM + r;
+          if (row < a.M) a.y[(size_t)e * a.stride + row] = (h0 + P[kOffB5]) + hs;
+        }
+      }
+    }
+    if (!ok && lane == 0) atomicExch(a.error, 13u);
+  }
+  __syncthreads();
+  if (warp == 1) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc(tmem, 2 * kTmemCols);
+  }
+}
+
+// ----------------------------------------------------------------------------
 // CUDA-core kernels around the GEMMs
 // ----------------------------------------------------------------------------
 

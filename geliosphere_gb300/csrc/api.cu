@@ -397,15 +397,32 @@ static int map_cuda_at(cudaError_t e, int line) {
     if (e_ != cudaSuccess) return map_cuda(e_); \
   } while (0)
 
+// Grow a device buffer: the larger buffer is allocated before the old one is
+// released, so a refused or failed allocation leaves the context with the
+// buffers (and the cached graph) it had.
 template <class T>
 static cudaError_t grow(T *&ptr, size_t &cap_bytes, size_t need_bytes) {
   if (need_bytes <= cap_bytes && ptr != nullptr) return cudaSuccess;
+  T *fresh = nullptr;
+  cudaError_t e = dev_malloc(&fresh, need_bytes);
+  if (e != cudaSuccess) return e;
   if (ptr) cudaFree(ptr);
-  ptr = nullptr;
-  cap_bytes = 0;
-  cudaError_t e = dev_malloc(&ptr, need_bytes);
-  if (e == cudaSuccess) cap_bytes = need_bytes;
-  return e;
+  ptr = fresh;
+  cap_bytes = need_bytes;
+  return cudaSuccess;
+}
+
+// Pinned host staging, grown the same way.
+template <class T>
+static cudaError_t grow_pinned(T *&ptr, int &cap, int need) {
+  if (need <= cap && ptr != nullptr) return cudaSuccess;
+  T *fresh = nullptr;
+  cudaError_t e = pinned_malloc(&fresh, sizeof(T) * (size_t)need);
+  if (e != cudaSuccess) return e;
+  if (ptr) cudaFreeHost(ptr);
+  ptr = fresh;
+  cap = need;
+  return cudaSuccess;
 }
 
 static void release(gelio_ctx *c) {
@@ -421,18 +438,29 @@ static void release(gelio_ctx *c) {
   if (c->stream) cudaStreamDestroy(c->stream);
 }
 
+// Per-simulation buffers for n simulations: all five new buffers are
+// allocated before the old ones are released, so a refused or failed
+// allocation leaves the context as it was.
 static int ensure_sims(gelio_ctx *c, int n) {
   if (n <= c->cap_sims) return GELIO_OK;
   int cap = 16;
   while (cap < n) cap *= 2;
+  gelio_sim_params *params = nullptr;
+  SimDev *sims = nullptr;
+  float *tables = nullptr;
+  int *gsim = nullptr;
+  unsigned long long *gpre = nullptr;
+  cudaError_t e = dev_malloc(&params, sizeof(gelio_sim_params) * cap);
+  if (e == cudaSuccess) e = dev_malloc(&sims, sizeof(SimDev) * cap);
+  if (e == cudaSuccess) e = dev_malloc(&tables, sizeof(float) * GELIO_GRID_MAX * cap);
+  if (e == cudaSuccess) e = dev_malloc(&gsim, sizeof(int) * 4 * cap);
+  if (e == cudaSuccess) e = dev_malloc(&gpre, sizeof(unsigned long long) * 4 * (cap + 1));
+  if (e != cudaSuccess) {
+    cudaFree(params); cudaFree(sims); cudaFree(tables); cudaFree(gsim); cudaFree(gpre);
+    return map_cuda(e);
+  }
   cudaFree(c->d_params); cudaFree(c->d_sims); cudaFree(c->d_tables); cudaFree(c->d_gsim); cudaFree(c->d_gpre);
-  c->d_params = nullptr; c->d_sims = nullptr; c->d_tables = nullptr; c->d_gsim = nullptr; c->d_gpre = nullptr;
-  c->cap_sims = 0;
-  GELIO_TRY(dev_malloc(&c->d_params, sizeof(gelio_sim_params) * cap));
-  GELIO_TRY(dev_malloc(&c->d_sims, sizeof(SimDev) * cap));
-  GELIO_TRY(dev_malloc(&c->d_tables, sizeof(float) * GELIO_GRID_MAX * cap));
-  GELIO_TRY(dev_malloc(&c->d_gsim, sizeof(int) * 4 * cap));
-  GELIO_TRY(dev_malloc(&c->d_gpre, sizeof(unsigned long long) * 4 * (cap + 1)));
+  c->d_params = params; c->d_sims = sims; c->d_tables = tables; c->d_gsim = gsim; c->d_gpre = gpre;
   c->cap_sims = cap;
   if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
   return GELIO_OK;
@@ -704,13 +732,7 @@ int32_t gelio_run(gelio_ctx *c, const gelio_sim_params *sims, int32_t n, const g
   if (stats) memset(stats, 0, sizeof(*stats));
   if (n == 0) return GELIO_OK;
   if ((rc = ensure_sims(c, n)) != GELIO_OK) return rc;
-  if (n > c->h_params_cap) {
-    if (c->h_params) cudaFreeHost(c->h_params);
-    c->h_params = nullptr;
-    c->h_params_cap = 0;
-    GELIO_TRY(pinned_malloc(&c->h_params, sizeof(gelio_sim_params) * c->cap_sims));
-    c->h_params_cap = c->cap_sims;
-  }
+  if (n > c->h_params_cap) GELIO_TRY(grow_pinned(c->h_params, c->h_params_cap, c->cap_sims));
   memcpy(c->h_params, sims, sizeof(gelio_sim_params) * n);
   unsigned mask = 0;
   int counts[4] = {0, 0, 0, 0};
@@ -731,14 +753,7 @@ int32_t gelio_run(gelio_ctx *c, const gelio_sim_params *sims, int32_t n, const g
     (unsigned long long)(o ? o->refill_interval : 0), (unsigned long long)rec_cap,
     (unsigned long long)(o ? o->max_steps_per_particle : 0),
     (unsigned long long)((o ? o->time_limit_s : 0.0) * 1e9)};
-  if (graph && n > c->h_out_cap) {
-    if (c->h_out) cudaFreeHost(c->h_out);
-    c->h_out = nullptr;
-    c->h_out_cap = 0;
-    if (c->graph) { cudaGraphExecDestroy(c->graph); c->graph = nullptr; }
-    GELIO_TRY(pinned_malloc(&c->h_out, sizeof(gelio_spectra) * c->cap_sims));
-    c->h_out_cap = c->cap_sims;
-  }
+  if (graph && n > c->h_out_cap) GELIO_TRY(grow_pinned(c->h_out, c->h_out_cap, c->cap_sims));
   if (graph) {
     // graphs copy through pinned staging (pageable host memory cannot be a
     // memcpy node); the staging pointer is fixed, so the graph is reusable

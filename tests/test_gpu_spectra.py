@@ -96,7 +96,12 @@ def test_2d_spectra_match_reference_cpu_model(engine, case):
     print(f"{case}: bins " + " ".join(f"{k} {v.size}" for k, v in z.items()) +
           f"; max|z| {np.abs(zall).max():.2f}; chi2/dof " + " ".join(f"{k} {v:.3f}" for k, v in chi2.items()) +
           f"; within 3 sigma {np.mean(np.abs(zall) < 3):.3f}")
-    assert z["weber"].size >= 12 and z["ams"].size >= 5 and z["ulysses"].size >= 1
+    if doc["resolved"]["useUniformInjection"]:
+        # the linear 0.0101 GeV grid fills only the SolarProp windows above
+        # ~0.5 GeV (each +-1% wide); the AMS bins carry the comparison
+        assert z["weber"].size >= 8 and z["ams"].size >= 40 and z["ulysses"].size >= 1
+    else:
+        assert z["weber"].size >= 12 and z["ams"].size >= 5 and z["ulysses"].size >= 1
     assert np.abs(zall).max() < 3.5
     assert max(chi2.values()) <= 1.2
 

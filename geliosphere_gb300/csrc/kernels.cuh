@@ -409,10 +409,33 @@ template <int MODEL> struct StepsPerCall {
   static constexpr int value = (MODEL == kModelGeliosphere) ? 1 : (MODEL == kModelSolarProp) ? 2 : 4;
 };
 
+// 2D Geliosphere draws three normals per step (the reference's other two
+// multiply B13 = B23 = 0).  Each group of four steps takes its twelve normals
+// from three Philox calls, counters 3 g, 3 g + 1, 3 g + 2 for group
+// g = step / 4: step 4 g + p uses normals 3 p .. 3 p + 2 of the group, and
+// the ones a call draws ahead are carried in the lane.  Particles start only
+// at refill boundaries (multiples of four steps), so the lanes of a warp
+// share the phase p and the fourth step's skipped draw is warp-uniform.
+template <class R>
+__device__ __forceinline__ void draw_geliosphere(Lane<R> &L, R *z) {
+  const uint32_t p = L.steps & 3u;
+  R a[4] = {R(0), R(0), R(0), R(0)};
+  if (p != 3u) normals4<R>(L.key0, L.key1, 3u * (L.steps >> 2) + p, kStreamSde, L.pid, a);
+  if (p == 0u) {
+    z[0] = a[0]; z[1] = a[1]; z[2] = a[2]; L.zc0 = a[3];
+  } else if (p == 1u) {
+    z[0] = L.zc0; z[1] = a[0]; z[2] = a[1]; L.zc0 = a[2]; L.zc1 = a[3];
+  } else if (p == 2u) {
+    z[0] = L.zc0; z[1] = L.zc1; z[2] = a[0]; L.zc0 = a[1]; L.zc1 = a[2]; L.zc2 = a[3];
+  } else {
+    z[0] = L.zc0; z[1] = L.zc1; z[2] = L.zc2;
+  }
+}
+
 template <int MODEL, class R>
-__device__ __forceinline__ void draw(const Lane<R> &L, R *z) {
+__device__ __forceinline__ void draw(Lane<R> &L, R *z) {
   if constexpr (MODEL == kModelGeliosphere) {
-    normals3<R>(L.key0, L.key1, L.steps, L.pid, z[0], z[1], z[2]);
+    draw_geliosphere<R>(L, z);
   } else {
     constexpr int spc = StepsPerCall<MODEL>::value;
     normals4<R>(L.key0, L.key1, L.steps / spc, kStreamSde, L.pid, z);
@@ -618,7 +641,9 @@ __global__ void __launch_bounds__(256, MINB) k_persistent(const KArgs a) {
             if (active) {
               const int res = model_step<MODEL, R>(L, K, z, j);
               ++L.steps;
-              if (res != kContinue) {
+              // one test per step covers the rare events: an exit, a stop,
+              // the step cap (an exit on the capped step counts as an exit)
+              if (res != kContinue || L.steps >= cap32) {
                 active = false;
                 sink.add(slot, L.sim, kOffNSteps, (double)L.steps);
                 if (res == kRecordAndStop) {
@@ -630,14 +655,11 @@ __global__ void __launch_bounds__(256, MINB) k_persistent(const KArgs a) {
                   e.slot_gbin = ((unsigned)(L.gbin + 1) << 16) | ((unsigned)slot & 0xffffu);
                   q[atomicAdd(qlen, 1)] = e;
                   if (a.records != nullptr) append_record_one(a, L, MODEL);
-                } else {
+                } else if (res != kContinue) {
                   sink.add(slot, L.sim, kOffNLost, 1.0);
+                } else {
+                  sink.add(slot, L.sim, kOffNCapped, 1.0);
                 }
-              }
-              if (active && L.steps >= a.max_steps) {
-                active = false;
-                sink.add(slot, L.sim, kOffNSteps, (double)L.steps);
-                sink.add(slot, L.sim, kOffNCapped, 1.0);
               }
             }
           }

@@ -88,28 +88,6 @@ __device__ __forceinline__ void normals4(uint32_t k0, uint32_t k1, uint32_t step
   box_muller((R)u32_to_unit(o.z), (R)u32_to_unit(o.w), z[2], z[3]);
 }
 
-// Three normals for one 2D-Geliosphere step: (A0, A1, B0).  The reference
-// draws five normals per step (GeliosphereModel.cu:291-303) but two of them
-// multiply B13 = B23 = 0 identically (Krph = Ktph = 0), so the unused sine of
-// pair B is not evaluated.
-template <class R>
-__device__ __forceinline__ void normals3(uint32_t k0, uint32_t k1, uint32_t step,
-                                         uint64_t particle, R &n1, R &n2, R &n4) {
-  Philox4 c;
-  c.x = step;
-  c.y = 0u;
-  c.z = (uint32_t)particle;
-  c.w = (uint32_t)(particle >> 32);
-  const Philox4 o = philox4x32_10(c, k0, k1);
-  box_muller((R)u32_to_unit(o.x), (R)u32_to_unit(o.y), n1, n2);
-  const R u1 = (R)u32_to_unit(o.z), u2 = (R)u32_to_unit(o.w);
-  if constexpr (sizeof(R) == 4) {
-    n4 = sqrtf(-2.0f * __logf(u1)) * cospif(2.0f * u2);
-  } else {
-    n4 = sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
-  }
-}
-
 // Stream ids of the counter's second word.
 constexpr uint32_t kStreamSde = 0u;
 constexpr uint32_t kStreamInjection = 1u;

@@ -189,6 +189,7 @@ template <class R> struct Lane {
   int gbin;
   unsigned long long pid;
   uint32_t key0, key1;
+  R zc0, zc1, zc2;     // 2D Geliosphere: normals drawn for the next steps of the group of four
 };
 
 // Outcome of one step.

@@ -183,10 +183,14 @@ void gpu_geliosphere(const gelio_sim_params &p, uint64_t pid, uint64_t max_steps
   double delta, deltarh, deltarh2, Krt, B11, B12, B22;
   double sin3, sin2, dKtt1, dKtt2, dKtt3, dKtt4, CKtt, dKrtr, dKrtt, dKper;
   uint32_t step = 0;
+  double grp[12];      // the twelve normals of the current group of four steps
   while (r < 100.0) {
     if (step >= max_steps) { t.status = 2; break; }
-    double z[4];
-    philox_normals(step, 0u, pid, key, z);
+    // group g = step / 4 draws counters 3g, 3g + 1, 3g + 2; step 4g + p
+    // takes normals 3p .. 3p + 2 of the group
+    if ((step & 3u) == 0u)
+      for (uint32_t k = 0; k < 3; ++k) philox_normals(3u * (step >> 2) + k, 0u, pid, key, grp + 4 * k);
+    const double *z = grp + 3 * (step & 3u);
     ++step;
     beta = std::sqrt(Tkin * (Tkin + T0 + T0)) / (Tkin + T0);
     Rig = std::sqrt(Tkin * (Tkin + (2.0 * T0)));

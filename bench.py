@@ -32,6 +32,9 @@ Other workloads (--workload; each prints its own line of the same form):
             `geliosphere -b` executable
   surrogate the MLP ensemble trained on MC spectra, timed against the MC on
             held-out draws (spectra/s, median flux error, tensor roofline)
+  surrogate_infer  inference alone: a 5-member ensemble with seeded random
+            weights answering 2,000 simulations x 100 grid points per step
+            (the surrogate workload's query), spectra/s and tensor roofline
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gelio|reference]
                        [--particles P] [--no-cpu-baseline] [--workload W]
@@ -80,7 +83,7 @@ def parse():
     ap.add_argument("--surr-epochs", type=int, default=60)
     ap.add_argument("--batch-scale", type=float, default=1.0, help="batch256: particle-count scale (profiling)")
     ap.add_argument("--workload", default="geliosphere",
-                    choices=["geliosphere", "bp", "fp", "batch256", "batch_cli", "surrogate"],
+                    choices=["geliosphere", "bp", "fp", "batch256", "batch_cli", "surrogate", "surrogate_infer"],
                     help="geliosphere: the headline 4-case 2D run (default); bp: 1D B-p 1e7 on a 100-point "
                          "log grid, FP32 and FP64 steps; fp: 1D F-p 1e6 log-uniform, 300 log bins; batch256: "
                          "256 random 2D simulations in one launch vs 256 plain launches; surrogate: train the "
@@ -582,6 +585,67 @@ def run_surrogate(args, eng, rank, world, local):
     sur.close()
 
 
+def run_surrogate_infer(args, eng, rank, world, local):
+    """Surrogate inference alone: 5 members with seeded random weights (the
+    architecture's sizes; inference cost does not depend on the values)
+    answering the held-out query of the surrogate workload, 2,000 simulations
+    x 100 log-grid points, every step.  value = spectra/s of predict through
+    the C ABI (host parameters in, host ratios and spread out); the roofline
+    is the fused network kernel's FLOP over the device time of each predict."""
+    import numpy as np
+    from geliosphere_gb300 import abi
+    from geliosphere_gb300 import surrogate as sg
+    members, n = 5, args.surr_test
+    sur = sg.Surrogate(eng, members=members, batch_rows=8192, seed=7 + rank)
+    rng = np.random.default_rng(123 + rank)
+    for m in range(members):
+        p = np.zeros(abi.GELIO_SURR_PARAMS, np.float32)
+        for k, (off, shape) in sg.OFFSETS.items():
+            size = int(np.prod(shape))
+            fan_in = shape[1] if len(shape) == 2 else 256
+            p[off:off + size] = (rng.normal(0, 0.05, size) if k.startswith("b") else
+                                 rng.uniform(-1, 1, size) * np.sqrt(3.0 / fan_in))
+        sur.set_params(m, p)
+    sims = random_2d_sims(n, 1, 10_000 + rank)
+    for _ in range(max(1, args.warmup)):
+        sur.predict(sims)
+    walls, devs = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        sur.predict(sims)
+        walls.append(time.perf_counter() - t0)
+        devs.append(sur.last_inference()[0])
+    _, flop = sur.last_inference()
+    peaks = {}
+    pfile = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pfile):
+        peaks = json.load(open(pfile))
+    bf16_peak = peaks.get("bf16_tflops", 1900.0)
+    dev_ms = statistics.mean(devs)
+    achieved = flop / (dev_ms / 1e3) / 1e12
+    wall = statistics.mean(walls)
+    sur.close()
+    if rank != 0:
+        return
+    rows = n * 100
+    line = {"metric": "surrogate inference spectra/s", "value": world * n / wall, "unit": "spectra/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": run_surrogate_infer.__doc__.replace("\n", " "), "members": members,
+                       "simulations": n, "rows": rows},
+            "device_ms_per_step": dev_ms, "wall_over_device": 1e3 * wall / dev_ms,
+            "e2e": {"value": world * n / wall, "unit": "spectra/s", "h2d_bytes_per_step": n * 96,
+                    "d2h_bytes_per_step": rows * 16},
+            "gpu_launches": (2 * -(-rows // 65536) + 1) * args.steps,
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
+                         "frac": achieved / bf16_peak, "traffic": None,
+                         "kernel": "k_mlp_infer_fused (tcgen05, all layers and members in one launch)",
+                         "flop_per_step": flop,
+                         "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if peaks else
+                                        "fallback 1.9 PFLOP/s bf16 burst"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
@@ -606,8 +670,9 @@ def main():
         return
     torch.cuda.set_device(local)
     eng = Engine(local)
-    if args.workload in ("batch256", "surrogate"):
-        (run_batch256 if args.workload == "batch256" else run_surrogate)(args, eng, rank, world, local)
+    if args.workload in ("batch256", "surrogate", "surrogate_infer"):
+        {"batch256": run_batch256, "surrogate": run_surrogate,
+         "surrogate_infer": run_surrogate_infer}[args.workload](args, eng, rank, world, local)
         eng.close()
         if world > 1:
             import torch.distributed as dist

@@ -379,10 +379,13 @@ struct gelio_ctx {
 // Text of the last CUDA failure seen by this thread (gelio_last_error).
 static thread_local char g_last_error[256] = "";
 
+void gelio::note_cuda_error(cudaError_t e, const char *file, int line) {
+  snprintf(g_last_error, sizeof(g_last_error), "%s (%s) at %s:%d", cudaGetErrorName(e), cudaGetErrorString(e), file,
+           line);
+}
+
 static int map_cuda_at(cudaError_t e, int line) {
-  if (e != cudaSuccess)
-    snprintf(g_last_error, sizeof(g_last_error), "%s (%s) at api.cu:%d", cudaGetErrorName(e),
-             cudaGetErrorString(e), line);
+  if (e != cudaSuccess) gelio::note_cuda_error(e, "api.cu", line);
   if (e == cudaSuccess) return GELIO_OK;
   if (e == cudaErrorMemoryAllocation) return GELIO_ERR_OUT_OF_MEMORY;
   if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver || e == cudaErrorInvalidDevice)

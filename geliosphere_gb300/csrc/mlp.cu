@@ -130,9 +130,8 @@ struct gelio_surrogate {
   size_t query_cap = 0;
   // predict: simulations and their row offsets on the device, member outputs
   // [E][stride], ensemble mean / std [2][rows], pinned staging of both ends
-  gelio_sim_params *d_psims = nullptr;
-  long long *d_pfirst = nullptr;
-  size_t psims_cap = 0;
+  unsigned char *d_pup = nullptr;     // [n] gelio_sim_params, then [n + 1] row offsets
+  size_t pup_cap = 0;
   float *d_py = nullptr;
   double *d_pstat = nullptr;
   size_t prows_cap = 0;
@@ -154,11 +153,13 @@ struct gelio_surrogate {
 
 namespace {
 
-int cuda_status(cudaError_t e) {
+int cuda_status_at(cudaError_t e, int line) {
   if (e == cudaSuccess) return GELIO_OK;
+  gelio::note_cuda_error(e, "mlp.cu", line);
   if (e == cudaErrorMemoryAllocation) return GELIO_ERR_OUT_OF_MEMORY;
   return GELIO_ERR_CUDA;
 }
+#define cuda_status(e) cuda_status_at((e), __LINE__)
 #define SUR_TRY(x)                            \
   do {                                        \
     cudaError_t e_ = (x);                     \
@@ -212,7 +213,7 @@ void free_all(gelio_surrogate *s) {
   f(s->yhat); f(s->y); f(s->dy); f(s->partial); f(s->grad); f(s->loss_part); f(s->step_loss);
   f(s->ident); f(s->order); f(s->error); f(s->d_feats); f(s->d_targ); f(s->d_query); f(s->d_yq);
   f(s->Q0); f(s->Q[0]); f(s->Q[1]); f(s->qy); f(s->qident);
-  f(s->d_psims); f(s->d_pfirst); f(s->d_py); f(s->d_pstat);
+  f(s->d_pup); f(s->d_py); f(s->d_pstat);
   if (s->h_pstage) cudaFreeHost(s->h_pstage);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
@@ -421,6 +422,7 @@ int32_t gelio_surrogate_create(gelio_ctx *ctx, const gelio_surrogate_opts *opts,
   int rc = GELIO_OK;
   auto fail = [&](int r) { free_all(s); delete s; return r; };
   if (cudaSetDevice(s->device) != cudaSuccess) return fail(GELIO_ERR_NO_DEVICE);
+  (void)cudaGetLastError();   // a launch check below must see only this call's errors
   if (!encode_fn()) return fail(GELIO_ERR_UNSUPPORTED);
   if ((rc = set_smem_attrs()) != GELIO_OK) return fail(rc);
   cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device);
@@ -571,6 +573,7 @@ int32_t gelio_surrogate_train(gelio_surrogate *s, int32_t epochs, float *last_lo
   const size_t nrow = s->targ.size();
   if (nrow == 0) return GELIO_ERR_NOT_TRAINED;
   SUR_TRY(cudaSetDevice(s->device));
+  (void)cudaGetLastError();   // a launch check below must see only this call's errors
   if (s->dirty) {
     if (nrow > s->d_rows_cap) {
       if (s->d_feats) cudaFree(s->d_feats);
@@ -681,16 +684,17 @@ int infer_sims(gelio_surrogate *s, const gelio_sim_params *sims, int n, size_t r
   const size_t stride = (rows + kTileM - 1) / kTileM * kTileM;
   const size_t up = (size_t)n * sizeof(gelio_sim_params) + (size_t)(n + 1) * sizeof(long long);
   const size_t down = 2 * rows * sizeof(double);
-  if ((size_t)n > s->psims_cap) {
-    if (s->d_psims) cudaFree(s->d_psims);
-    if (s->d_pfirst) cudaFree(s->d_pfirst);
-    s->d_psims = nullptr;
-    s->d_pfirst = nullptr;
-    s->psims_cap = 0;
-    SUR_TRY(gelio::dev_malloc(&s->d_psims, (size_t)n * sizeof(gelio_sim_params)));
-    SUR_TRY(gelio::dev_malloc(&s->d_pfirst, (size_t)(n + 1) * sizeof(long long)));
-    s->psims_cap = (size_t)n;
+  // the simulations and their row offsets travel in one copy, so they share
+  // one allocation (n * 96 bytes keeps the offsets 8-byte aligned)
+  if (up > s->pup_cap) {
+    unsigned char *fresh = nullptr;
+    SUR_TRY(gelio::dev_malloc(&fresh, up));
+    if (s->d_pup) cudaFree(s->d_pup);
+    s->d_pup = fresh;
+    s->pup_cap = up;
   }
+  const gelio_sim_params *d_psims = reinterpret_cast<const gelio_sim_params *>(s->d_pup);
+  const long long *d_pfirst = reinterpret_cast<const long long *>(s->d_pup + (size_t)n * sizeof(gelio_sim_params));
   if (stride > s->prows_cap) {
     if (s->d_py) cudaFree(s->d_py);
     if (s->d_pstat) cudaFree(s->d_pstat);
@@ -713,14 +717,13 @@ int infer_sims(gelio_surrogate *s, const gelio_sim_params *sims, int n, size_t r
   first[0] = 0;
   for (int i = 0; i < n; ++i) first[i + 1] = first[i] + sims[i].inj_points;
   SUR_TRY(cudaEventRecord(s->ev0, s->stream));
-  SUR_TRY(cudaMemcpyAsync(s->d_psims, s->h_pstage, up, cudaMemcpyHostToDevice, s->stream));
+  SUR_TRY(cudaMemcpyAsync(s->d_pup, s->h_pstage, up, cudaMemcpyHostToDevice, s->stream));
   size_t padded = 0;
   for (size_t off = 0; off < rows; off += (size_t)s->qrows) {
     const int c = (int)std::min<size_t>((size_t)s->qrows, rows - off);
     const int M = (c + kTileM - 1) / kTileM * kTileM;
     padded += (size_t)(c + 2 * kTileM - 1) / (2 * kTileM) * (2 * kTileM);   // rows the fused kernel multiplies
-    k_query_features<<<(M + 127) / 128, 128, 0, s->stream>>>(s->d_psims, s->d_pfirst, n, (long long)off, c, M,
-                                                             s->Q0);
+    k_query_features<<<(M + 127) / 128, 128, 0, s->stream>>>(d_psims, d_pfirst, n, (long long)off, c, M, s->Q0);
     SUR_TRY(cudaGetLastError());
     const int rc = infer_fused(s, c, s->d_py + off, (long long)stride);
     if (rc != GELIO_OK) return rc;
@@ -749,6 +752,7 @@ int32_t gelio_surrogate_forward(gelio_surrogate *s, int32_t member, const float 
   if (!valid_member(s, member) || n < 0 || (n > 0 && (!x || !y))) return GELIO_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lock(s->mu);
   SUR_TRY(cudaSetDevice(s->device));
+  (void)cudaGetLastError();   // a launch check below must see only this call's errors
   return infer_rows(s, member, member + 1, x, (size_t)n, y);
 }
 
@@ -758,6 +762,7 @@ int32_t gelio_surrogate_gradient(gelio_surrogate *s, int32_t member, const float
   std::lock_guard<std::mutex> lock(s->mu);
   if (n > s->rows) return GELIO_ERR_INVALID_ARGUMENT;
   SUR_TRY(cudaSetDevice(s->device));
+  (void)cudaGetLastError();   // a launch check below must see only this call's errors
   float *d_x = nullptr, *d_t = nullptr, *d_loss = nullptr;
   int rc = GELIO_OK;
   if (gelio::dev_malloc(&d_x, (size_t)n * kFeatures * 4) != cudaSuccess || gelio::dev_malloc(&d_t, (size_t)n * 4) != cudaSuccess ||
@@ -795,6 +800,7 @@ int32_t gelio_surrogate_get_params(gelio_surrogate *s, int32_t member, float *pa
   if (!valid_member(s, member) || !params) return GELIO_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lock(s->mu);
   SUR_TRY(cudaSetDevice(s->device));
+  (void)cudaGetLastError();   // a launch check below must see only this call's errors
   SUR_TRY(cudaMemcpyAsync(params, s->mem[member].P, (size_t)kParams * 4, cudaMemcpyDeviceToHost, s->stream));
   SUR_TRY(cudaStreamSynchronize(s->stream));
   return GELIO_OK;
@@ -804,6 +810,7 @@ int32_t gelio_surrogate_set_params(gelio_surrogate *s, int32_t member, const flo
   if (!valid_member(s, member) || !params) return GELIO_ERR_INVALID_ARGUMENT;
   std::lock_guard<std::mutex> lock(s->mu);
   SUR_TRY(cudaSetDevice(s->device));
+  (void)cudaGetLastError();   // a launch check below must see only this call's errors
   Member &m = s->mem[member];
   SUR_TRY(cudaMemcpyAsync(m.P, params, (size_t)kParams * 4, cudaMemcpyHostToDevice, s->stream));
   SUR_TRY(cudaMemsetAsync(m.M1, 0, (size_t)kParams * 4, s->stream));
@@ -831,6 +838,7 @@ int32_t gelio_surrogate_predict(gelio_surrogate *s, const gelio_sim_params *sims
   if (rows == 0) return GELIO_OK;
   std::lock_guard<std::mutex> lock(s->mu);
   SUR_TRY(cudaSetDevice(s->device));
+  (void)cudaGetLastError();   // a launch check below must see only this call's errors
   return infer_sims(s, sims, n, rows, ln_ratio, ln_std);
 }
 

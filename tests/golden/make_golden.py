@@ -13,7 +13,7 @@ oracle/Makefile target `ref` into oracle/_ref/, never committed):
   weights, of squared weights and counts) at larger N, evaluated with the
   oracle evaluator pinned above: the statistical target of the GPU tests.
 
-usage: python tests/golden/make_golden.py [--skip-spectra]
+usage: python tests/golden/make_golden.py [--skip-spectra] [--spectra=case,...] [--second-sample]
 """
 from __future__ import annotations
 
@@ -210,15 +210,21 @@ def spectra_goldens():
         "solarprop_r70_th160_a_neg_tilt70": ("solarprop", base_args(500, 70, -1, 0, r=70, theta=160), 48),
     }
     only = [a.split("=", 1)[1].split(",") for a in sys.argv if a.startswith("--spectra=")]
+    # --second-sample: an independent reference sample of every 2D case
+    # (seeds 100001 + block instead of 1 + block), written as
+    # ref_spectra_<case>_b.json; the 2D tests pool it with the first sample
+    second = "--second-sample" in sys.argv
     for name, (model, args, nb) in cases.items():
         if only and name not in only[0]:
             continue
-        resolved, n_rec, arr, n_traj = spectra_case(model, args, nb)
+        if second and model not in ("geliosphere", "solarprop"):
+            continue
+        resolved, n_rec, arr, n_traj = spectra_case(model, args, nb, seed0=100001 if second else 1)
         doc = {"model": model, "args": args, "resolved": resolved, "n_records": n_rec,
                "n_trajectories": n_traj, "spectra": arr}
-        with open(os.path.join(HERE, f"ref_spectra_{name}.json"), "w") as f:
+        with open(os.path.join(HERE, f"ref_spectra_{name}{'_b' if second else ''}.json"), "w") as f:
             json.dump(doc, f)
-        print("spectra", name, n_rec, n_traj)
+        print("spectra", name, "second sample" if second else "", n_rec, n_traj, flush=True)
 
 
 def main():

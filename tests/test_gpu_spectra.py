@@ -65,8 +65,24 @@ def compare_sections(gpu, ref, sections, min_count=200):
 
 
 TWO_D_CASES = sorted(os.path.basename(f)[len("ref_spectra_"):-len(".json")]
-                     for f in os.listdir(GOLDEN) if f.startswith("ref_spectra_") and
-                     f.startswith(("ref_spectra_geliosphere", "ref_spectra_solarprop")))
+                     for f in os.listdir(GOLDEN) if f.startswith(("ref_spectra_geliosphere", "ref_spectra_solarprop"))
+                     and not f.endswith("_b.json"))
+
+
+def load_reference(case):
+    """The reference fixture of a 2D case, pooled with its independent second
+    sample (ref_spectra_<case>_b.json, other seeds) when present: the
+    per-bin sums of weights, squared weights and counts add."""
+    doc = json.load(open(os.path.join(GOLDEN, f"ref_spectra_{case}.json")))
+    second = os.path.join(GOLDEN, f"ref_spectra_{case}_b.json")
+    if os.path.exists(second):
+        b = json.load(open(second))
+        assert b["resolved"] == doc["resolved"]
+        doc["spectra"] = {k: (np.add(v, b["spectra"][k]).tolist() if isinstance(v, list) else v + b["spectra"][k])
+                          for k, v in doc["spectra"].items()}
+        doc["n_trajectories"] += b["n_trajectories"]
+        doc["samples"] = 2
+    return doc
 
 
 @pytest.mark.parametrize("case", TWO_D_CASES)
@@ -74,9 +90,10 @@ def test_2d_spectra_match_reference_cpu_model(engine, case):
     """Every 2D reference fixture: the four (polarity, tilt) cases of the 2D
     workload at r 1 AU, theta 90 deg, and injections off the equator and
     beyond 1 AU (r 5-70 AU, theta 30-160 deg) for both 2D models, on the
-    SolarProp grid or on the CPU models' linear grid ("_uni").  Compared:
-    the SolarProp section (three LIS), the Ulysses bins and the AMS bins."""
-    doc = json.load(open(os.path.join(GOLDEN, f"ref_spectra_{case}.json")))
+    SolarProp grid or on the CPU models' linear grid ("_uni"), each pooled
+    from two independent reference samples where both exist.  Compared: the
+    SolarProp section (three LIS), the Ulysses bins and the AMS bins."""
+    doc = load_reference(case)
     sim = sim_from_fixture(doc, 3_000_000, seed=2024)
     gpu = spectra_dict(engine.run(sim).spectra[0])
     ref = doc["spectra"]
@@ -93,7 +110,8 @@ def test_2d_spectra_match_reference_cpu_model(engine, case):
     chi2 = {"weber": float(np.mean(z["weber"] ** 2))}
     if z["ams"].size >= 20:
         chi2["ams"] = float(np.mean(z["ams"] ** 2))
-    print(f"{case}: bins " + " ".join(f"{k} {v.size}" for k, v in z.items()) +
+    print(f"{case} (reference samples {doc.get('samples', 1)}, {doc['n_trajectories']} trajectories): bins " +
+          " ".join(f"{k} {v.size}" for k, v in z.items()) +
           f"; max|z| {np.abs(zall).max():.2f}; chi2/dof " + " ".join(f"{k} {v:.3f}" for k, v in chi2.items()) +
           f"; within 3 sigma {np.mean(np.abs(zall) < 3):.3f}")
     if doc["resolved"]["useUniformInjection"]:

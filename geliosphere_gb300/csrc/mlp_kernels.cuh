@@ -393,7 +393,9 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
 // [256 N][64 K], TMA from L2, a 2-stage ring) are loaded.
 //   warp 0 (one lane)  TMA: the item's two input tiles, then 13 weight chunks
 //   warp 1 (one lane)  MMA: per layer and K-chunk one N = 256 product per tile
-//                      into that tile's TMEM accumulator (2 x 256 columns)
+//                      into that tile's TMEM accumulator (2 x 256 columns),
+//                      the tiles staggered by two chunks so that one tile's
+//                      epilogue runs under the other tile's products
 //   warps 2-9          epilogue: warp w takes TMEM lane quarter w % 4 of
 //                      tile (w - 2) / 4, all 256 columns of its 32 rows
 // Every value equals the layer-by-layer INFER / INFER_LAST path bit for bit:
@@ -440,9 +442,9 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   uint64_t *empty = full + kFusedStages;
   uint64_t *a_full = empty + kFusedStages;      // the item's input tiles landed
   uint64_t *a_empty = a_full + 1;               // the item's last products read A
-  uint64_t *acc_full = a_empty + 1;             // a layer's products are in TMEM
-  uint64_t *acc_empty = acc_full + 1;           // a layer's epilogue read TMEM and wrote A
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(acc_empty + 1);
+  uint64_t *acc_full = a_empty + 1;             // [tile]: a layer's products are in TMEM
+  uint64_t *acc_empty = acc_full + 2;           // [tile]: a layer's epilogue read TMEM and wrote A
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(acc_empty + 2);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int items = a.E * a.n_pairs;
@@ -453,8 +455,10 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     }
     tc::mbar_init(a_full, 1);
     tc::mbar_init(a_empty, 1);
-    tc::mbar_init(acc_full, 1);
-    tc::mbar_init(acc_empty, kEpiWarps);
+    for (int t = 0; t < 2; ++t) {
+      tc::mbar_init(&acc_full[t], 1);
+      tc::mbar_init(&acc_empty[t], kEpiWarps / 2);
+    }
     tc::fence_mbar_init();
     tc::tma_prefetch(&maps.q0);
   }
@@ -512,28 +516,46 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       for (int w = blockIdx.x; w < items && ok; w += gridDim.x, ++local) {
         if (!tc::mbar_wait(a_full, local & 1, deadline)) { ok = false; break; }
         for (int l = 0; l < 4 && ok; ++l, ++layer) {
-          // the previous layer's epilogue has read TMEM and written A
-          if (layer > 0 && !tc::mbar_wait(acc_empty, (layer - 1) & 1, deadline)) { ok = false; break; }
-          tc::tc_fence_after();
+          // Issue order per layer (K chunks c0..c3, tiles X, Y sharing each
+          // chunk's stage): X c0 c1, Y c0 c1, X c2 c3, Y c2 c3.  X's products
+          // are complete two chunks before Y's, so X's epilogue overlaps Y's
+          // last products and Y's epilogue the next layer's first products
+          // of X.  Each tile's previous epilogue must have read its TMEM
+          // accumulator and written its A before the tile's first product.
           const int nk = (l == 0) ? 1 : kWidth / kChunk;
-          for (int kc = 0; kc < nk; ++kc) {
-            const uint32_t st = it % kFusedStages;
-            if (!tc::mbar_wait(&full[st], (it / kFusedStages) & 1, deadline)) { ok = false; break; }
-            tc::tc_fence_after();
+          auto mma_tile = [&](int t, int kc, uint32_t st) {
+            const uint32_t aa = tc::smem_u32(base + t * kFusedA + kc * kStageA);
             const uint32_t bb = tc::smem_u32(ring + st * kStageB);
 #pragma unroll
-            for (int t = 0; t < 2; ++t) {
-              const uint32_t aa = tc::smem_u32(base + t * kFusedA + kc * kStageA);
-#pragma unroll
-              for (int k = 0; k < kChunk / 16; ++k)
-                tc::mma_bf16(tmem + (uint32_t)t * kTmemCols, tc::sdesc_sw128(aa + k * 32),
-                             tc::sdesc_sw128(bb + k * 32), idesc, (kc > 0 || k > 0) ? 1u : 0u);
+            for (int k = 0; k < kChunk / 16; ++k)
+              tc::mma_bf16(tmem + (uint32_t)t * kTmemCols, tc::sdesc_sw128(aa + k * 32), tc::sdesc_sw128(bb + k * 32),
+                           idesc, (kc > 0 || k > 0) ? 1u : 0u);
+          };
+          if (layer > 0 && !tc::mbar_wait(&acc_empty[0], (layer - 1) & 1, deadline)) { ok = false; break; }
+          tc::tc_fence_after();
+          for (int g = 0; g < nk && ok; g += 2) {
+            const int cnt = min(2, nk - g);
+            for (int j = 0; j < cnt; ++j) {
+              const uint32_t st = (it + j) % kFusedStages;
+              if (!tc::mbar_wait(&full[st], ((it + j) / kFusedStages) & 1, deadline)) { ok = false; break; }
+              tc::tc_fence_after();
+              mma_tile(0, g + j, st);
             }
-            tc::mma_commit(&empty[st]);
-            ++it;
+            if (!ok) break;
+            if (g + cnt == nk) tc::mma_commit(&acc_full[0]);
+            if (g == 0) {
+              if (layer > 0 && !tc::mbar_wait(&acc_empty[1], (layer - 1) & 1, deadline)) { ok = false; break; }
+              tc::tc_fence_after();
+            }
+            for (int j = 0; j < cnt; ++j) {
+              const uint32_t st = (it + j) % kFusedStages;
+              mma_tile(1, g + j, st);
+              tc::mma_commit(&empty[st]);
+            }
+            it += cnt;
           }
           if (!ok) break;
-          tc::mma_commit(acc_full);
+          tc::mma_commit(&acc_full[1]);
           if (l == 3) tc::mma_commit(a_empty);
         }
       }
@@ -569,7 +591,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       }
       named_sync(1, 32 * kEpiWarps);
       for (int l = 0; l < 4; ++l, ++layer) {
-        if (ok) ok = __all_sync(0xffffffffu, tc::mbar_wait(acc_full, layer & 1, deadline));
+        if (ok) ok = __all_sync(0xffffffffu, tc::mbar_wait(&acc_full[t], layer & 1, deadline));
         if (!ok) continue;
         tc::tc_fence_after();
         float h0 = 0.0f, hs = 0.0f;            // head: columns 0-127, then the running half
@@ -597,7 +619,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         if (l < 3) fence_proxy_async_smem();     // A written for the tensor core
         tc::tc_fence_before();
         __syncwarp();
-        if (lane == 0) tc::mbar_arrive(acc_empty);
+        if (lane == 0) tc::mbar_arrive(&acc_empty[t]);
         if (l == 3) {
           const int row = pair * 2 * kTileM + t * kTileM + r;
           if (row < a.M) a.y[(size_t)e * a.stride + row] = (h0 + P[kOffB5]) + hs;

@@ -580,9 +580,10 @@ def run_surrogate(args, eng, rank, world, local):
             "e2e": {"value": sur_rate, "unit": "spectra/s",
                     "h2d_bytes_per_step": len(test) * 100 * 7 * 4,
                     "d2h_bytes_per_step": len(test) * 100 * 5 * 4},
-            # per 65,536-row inference batch: the query features and the fused
-            # network (every member); then the ensemble statistics
-            "gpu_launches": 2 * -(-len(test) * 100 // 65536) + 1,
+            # the per-simulation query inputs; per 65,536-row inference batch the
+            # per-row inputs and the fused network (every member); the ensemble
+            # statistics
+            "gpu_launches": 2 * -(-len(test) * 100 // 65536) + 2,
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
                          "frac": achieved / bf16_peak, "traffic": None, "kernel": "k_mlp_infer_fused (tcgen05, all layers and members in one launch)",
                          "device_ms": dev_ms, "flop": flop,
@@ -646,7 +647,7 @@ def run_surrogate_infer(args, eng, rank, world, local):
             "device_ms_per_step": dev_ms, "wall_over_device": 1e3 * wall / dev_ms,
             "e2e": {"value": world * n / wall, "unit": "spectra/s", "h2d_bytes_per_step": n * 96,
                     "d2h_bytes_per_step": rows * 16},
-            "gpu_launches": (2 * -(-rows // 65536) + 1) * args.steps,
+            "gpu_launches": (2 * -(-rows // 65536) + 2) * args.steps,
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
                          "frac": achieved / bf16_peak, "traffic": None,
                          "kernel": "k_mlp_infer_fused (tcgen05, all layers and members in one launch)",

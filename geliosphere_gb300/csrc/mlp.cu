@@ -682,19 +682,24 @@ int infer_sims(gelio_surrogate *s, const gelio_sim_params *sims, int n, size_t r
                double *ln_std) {
   const size_t E = s->mem.size();
   const size_t stride = (rows + kTileM - 1) / kTileM * kTileM;
+  // device layout: [n] gelio_sim_params, [n + 1] row offsets (both uploaded
+  // in one copy), then [n] QuerySim built on the device
   const size_t up = (size_t)n * sizeof(gelio_sim_params) + (size_t)(n + 1) * sizeof(long long);
+  const size_t qoff = (up + 63) / 64 * 64;
   const size_t down = 2 * rows * sizeof(double);
   // the simulations and their row offsets travel in one copy, so they share
   // one allocation (n * 96 bytes keeps the offsets 8-byte aligned)
-  if (up > s->pup_cap) {
+  const size_t dev_bytes = qoff + (size_t)n * sizeof(QuerySim);
+  if (dev_bytes > s->pup_cap) {
     unsigned char *fresh = nullptr;
-    SUR_TRY(gelio::dev_malloc(&fresh, up));
+    SUR_TRY(gelio::dev_malloc(&fresh, dev_bytes));
     if (s->d_pup) cudaFree(s->d_pup);
     s->d_pup = fresh;
-    s->pup_cap = up;
+    s->pup_cap = dev_bytes;
   }
   const gelio_sim_params *d_psims = reinterpret_cast<const gelio_sim_params *>(s->d_pup);
   const long long *d_pfirst = reinterpret_cast<const long long *>(s->d_pup + (size_t)n * sizeof(gelio_sim_params));
+  QuerySim *d_pq = reinterpret_cast<QuerySim *>(s->d_pup + qoff);
   if (stride > s->prows_cap) {
     if (s->d_py) cudaFree(s->d_py);
     if (s->d_pstat) cudaFree(s->d_pstat);
@@ -718,12 +723,14 @@ int infer_sims(gelio_surrogate *s, const gelio_sim_params *sims, int n, size_t r
   for (int i = 0; i < n; ++i) first[i + 1] = first[i] + sims[i].inj_points;
   SUR_TRY(cudaEventRecord(s->ev0, s->stream));
   SUR_TRY(cudaMemcpyAsync(s->d_pup, s->h_pstage, up, cudaMemcpyHostToDevice, s->stream));
+  k_query_sims<<<(n + 127) / 128, 128, 0, s->stream>>>(d_psims, n, d_pq);
+  SUR_TRY(cudaGetLastError());
   size_t padded = 0;
   for (size_t off = 0; off < rows; off += (size_t)s->qrows) {
     const int c = (int)std::min<size_t>((size_t)s->qrows, rows - off);
     const int M = (c + kTileM - 1) / kTileM * kTileM;
     padded += (size_t)(c + 2 * kTileM - 1) / (2 * kTileM) * (2 * kTileM);   // rows the fused kernel multiplies
-    k_query_features<<<(M + 127) / 128, 128, 0, s->stream>>>(d_psims, d_pfirst, n, (long long)off, c, M, s->Q0);
+    k_query_features<<<(M + 127) / 128, 128, 0, s->stream>>>(d_pq, d_pfirst, n, (long long)off, c, M, s->Q0);
     SUR_TRY(cudaGetLastError());
     const int rc = infer_fused(s, c, s->d_py + off, (long long)stride);
     if (rc != GELIO_OK) return rc;

@@ -772,28 +772,44 @@ __global__ void k_pack(const float *__restrict__ p, __nv_bfloat16 *__restrict__ 
 // Inference queries built on the device (gelio_surrogate_predict).
 // ---------------------------------------------------------------------------
 
-// Network input of grid point j of simulation s: the LOG_GRID energy as the
-// SDE kernels build it (FP64 log / exp, rounded to FP32) and the
-// normalisation of gelio_surrogate_features, evaluated in FP64 and rounded
-// to FP32 like the host function.
-__device__ __forceinline__ void query_features(const gelio_sim_params &s, int j, float f[kFeatures]) {
-  const double lmin = log((double)s.inj_min), lmax = log((double)s.inj_max);
-  const double fr = (s.inj_points > 1) ? (double)j / (double)(s.inj_points - 1) : 0.0;
-  const float T = (float)exp(lmin + fr * (lmax - lmin));
+// One simulation of a predict query, prepared once per simulation by
+// k_query_sims: its six network inputs that do not depend on the energy and
+// its LOG_GRID range.
+struct QuerySim {
+  float f[6];
+  int points;
+  float pad;
+  double lmin, lmax;       // log of the grid's lowest and highest energy
+};
+static_assert(sizeof(QuerySim) == 48, "QuerySim is staged as 48-byte records");
+
+// The normalisation of gelio_surrogate_features, evaluated in FP64 and
+// rounded to FP32 as the host function does, one thread per simulation.
+__global__ void k_query_sims(const gelio_sim_params *__restrict__ sims, int n, QuerySim *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const gelio_sim_params s = sims[i];
   const double rad = 180.0 / 3.14159265358979323846;
-  f[0] = (float)((log10((double)s.K0 / 4.4683705e-27) - 22.5) * 2.0);
-  f[1] = (float)(((double)s.V / 6.68458712e-9 - 550.0) / 200.0);
-  f[2] = (float)(((double)s.tilt * rad - 40.0) / 35.0);
-  f[3] = (float)s.polarity;
-  f[4] = (float)(((double)s.r_injection - 40.5) / 39.5);
-  f[5] = (float)(((double)s.theta_injection * rad - 90.0) / 80.0);
-  f[6] = (float)(log10((double)T) / 2.0);
+  QuerySim q;
+  q.f[0] = (float)((log10((double)s.K0 / 4.4683705e-27) - 22.5) * 2.0);
+  q.f[1] = (float)(((double)s.V / 6.68458712e-9 - 550.0) / 200.0);
+  q.f[2] = (float)(((double)s.tilt * rad - 40.0) / 35.0);
+  q.f[3] = (float)s.polarity;
+  q.f[4] = (float)(((double)s.r_injection - 40.5) / 39.5);
+  q.f[5] = (float)(((double)s.theta_injection * rad - 90.0) / 80.0);
+  q.points = s.inj_points;
+  q.pad = 0.f;
+  q.lmin = log((double)s.inj_min);
+  q.lmax = log((double)s.inj_max);
+  out[i] = q;
 }
 
 // Rows [off, off + c) of the query (row = first[i] + j: grid point j of
 // simulation i) into the BF16 first-layer operand x0 [M][kInPad]; rows c..M-1
-// of the tile padding are zero.
-__global__ void k_query_features(const gelio_sim_params *__restrict__ sims, const long long *__restrict__ first,
+// of the tile padding are zero.  Per row only the energy input is computed:
+// the LOG_GRID energy as the SDE kernels build it (FP64 exp, rounded to FP32)
+// and log10 of it / 2, as gelio_surrogate_features.
+__global__ void k_query_features(const QuerySim *__restrict__ sims, const long long *__restrict__ first,
                                  int n_sims, long long off, int c, int M, __nv_bfloat16 *__restrict__ x0) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= M) return;
@@ -805,7 +821,13 @@ __global__ void k_query_features(const gelio_sim_params *__restrict__ sims, cons
       const int mid = (lo + hi + 1) >> 1;
       if (first[mid] <= row) lo = mid; else hi = mid - 1;
     }
-    query_features(sims[lo], (int)(row - first[lo]), f);
+    const QuerySim q = sims[lo];
+    const int j = (int)(row - first[lo]);
+    const double fr = (q.points > 1) ? (double)j / (double)(q.points - 1) : 0.0;
+    const float T = (float)exp(q.lmin + fr * (q.lmax - q.lmin));
+#pragma unroll
+    for (int k = 0; k < 6; ++k) f[k] = q.f[k];
+    f[6] = (float)(log10((double)T) / 2.0);
   }
 #pragma unroll
   for (int k = 0; k < kFeatures; ++k) x0[(size_t)m * kInPad + k] = __float2bfloat16_rn(f[k]);

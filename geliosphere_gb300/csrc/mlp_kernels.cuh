@@ -595,10 +595,18 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         if (!ok) continue;
         tc::tc_fence_after();
         float h0 = 0.0f, hs = 0.0f;            // head: columns 0-127, then the running half
+        // 32-column chunks of the accumulator, the next chunk's TMEM load in
+        // flight while this one is evaluated
+        uint32_t buf[2][32];
+        tc::tmem_ld32_issue(trow, buf[0]);
+        tc::tmem_wait_ld(buf[0]);
+#pragma unroll
         for (int c = 0; c < kWidth / 32; ++c) {
+          if (c + 1 < kWidth / 32) tc::tmem_ld32_issue(trow + (uint32_t)((c + 1) * 32), buf[(c + 1) & 1]);
           if (c == 4) { h0 = hs; hs = 0.0f; }
           float v[32];
-          tc::tmem_ld32(trow + (uint32_t)(c * 32), v);
+#pragma unroll
+          for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(buf[c & 1][j]);
           __align__(16) __nv_bfloat16 out[32];
           silu_infer32(v, &s_b[l][c * 32], out);
           if (l == 3) {
@@ -615,6 +623,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
               *reinterpret_cast<uint4 *>(chunk + piece * 16) = src[i];
             }
           }
+          if (c + 1 < kWidth / 32) tc::tmem_wait_ld(buf[(c + 1) & 1]);
         }
         if (l < 3) fence_proxy_async_smem();     // A written for the tensor core
         tc::tc_fence_before();

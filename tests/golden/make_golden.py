@@ -13,7 +13,7 @@ oracle/Makefile target `ref` into oracle/_ref/, never committed):
   weights, of squared weights and counts) at larger N, evaluated with the
   oracle evaluator pinned above: the statistical target of the GPU tests.
 
-usage: python tests/golden/make_golden.py [--skip-spectra] [--spectra=case,...] [--second-sample]
+usage: python tests/golden/make_golden.py [--skip-spectra] [--spectra=case,...] [--second-sample | --third-sample]
 """
 from __future__ import annotations
 
@@ -210,21 +210,24 @@ def spectra_goldens():
         "solarprop_r70_th160_a_neg_tilt70": ("solarprop", base_args(500, 70, -1, 0, r=70, theta=160), 48),
     }
     only = [a.split("=", 1)[1].split(",") for a in sys.argv if a.startswith("--spectra=")]
-    # --second-sample: an independent reference sample of every 2D case
-    # (seeds 100001 + block instead of 1 + block), written as
-    # ref_spectra_<case>_b.json; the 2D tests pool it with the first sample
-    second = "--second-sample" in sys.argv
+    # --second-sample / --third-sample: independent reference samples of
+    # every 2D case (seeds 100001 + block / 200001 + block instead of
+    # 1 + block), written as ref_spectra_<case>_b.json / _c.json; the 2D
+    # tests pool every sample of a case
+    extra = "_b" if "--second-sample" in sys.argv else "_c" if "--third-sample" in sys.argv else ""
+    second = bool(extra)
     for name, (model, args, nb) in cases.items():
         if only and name not in only[0]:
             continue
         if second and model not in ("geliosphere", "solarprop"):
             continue
-        resolved, n_rec, arr, n_traj = spectra_case(model, args, nb, seed0=100001 if second else 1)
+        resolved, n_rec, arr, n_traj = spectra_case(model, args, nb,
+                                                    seed0={"": 1, "_b": 100001, "_c": 200001}[extra])
         doc = {"model": model, "args": args, "resolved": resolved, "n_records": n_rec,
                "n_trajectories": n_traj, "spectra": arr}
-        with open(os.path.join(HERE, f"ref_spectra_{name}{'_b' if second else ''}.json"), "w") as f:
+        with open(os.path.join(HERE, f"ref_spectra_{name}{extra}.json"), "w") as f:
             json.dump(doc, f)
-        print("spectra", name, "second sample" if second else "", n_rec, n_traj, flush=True)
+        print("spectra", name, extra, n_rec, n_traj, flush=True)
 
 
 def main():

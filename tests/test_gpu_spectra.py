@@ -66,22 +66,25 @@ def compare_sections(gpu, ref, sections, min_count=200):
 
 TWO_D_CASES = sorted(os.path.basename(f)[len("ref_spectra_"):-len(".json")]
                      for f in os.listdir(GOLDEN) if f.startswith(("ref_spectra_geliosphere", "ref_spectra_solarprop"))
-                     and not f.endswith("_b.json"))
+                     and not f.endswith(("_b.json", "_c.json")))
 
 
 def load_reference(case):
-    """The reference fixture of a 2D case, pooled with its independent second
-    sample (ref_spectra_<case>_b.json, other seeds) when present: the
-    per-bin sums of weights, squared weights and counts add."""
+    """The reference fixture of a 2D case, pooled with its independent further
+    samples (ref_spectra_<case>_b.json, _c.json: other seeds) where present:
+    the per-bin sums of weights, squared weights and counts add."""
     doc = json.load(open(os.path.join(GOLDEN, f"ref_spectra_{case}.json")))
-    second = os.path.join(GOLDEN, f"ref_spectra_{case}_b.json")
-    if os.path.exists(second):
-        b = json.load(open(second))
+    doc["samples"] = 1
+    for extra in ("_b", "_c"):
+        path = os.path.join(GOLDEN, f"ref_spectra_{case}{extra}.json")
+        if not os.path.exists(path):
+            continue
+        b = json.load(open(path))
         assert b["resolved"] == doc["resolved"]
         doc["spectra"] = {k: (np.add(v, b["spectra"][k]).tolist() if isinstance(v, list) else v + b["spectra"][k])
                           for k, v in doc["spectra"].items()}
         doc["n_trajectories"] += b["n_trajectories"]
-        doc["samples"] = 2
+        doc["samples"] += 1
     return doc
 
 

@@ -221,10 +221,10 @@ def spectra_goldens():
             continue
         if second and model not in ("geliosphere", "solarprop"):
             continue
-        resolved, n_rec, arr, n_traj = spectra_case(model, args, nb,
-                                                    seed0={"": 1, "_b": 100001, "_c": 200001}[extra])
+        seed0 = {"": 1, "_b": 100001, "_c": 200001}[extra]
+        resolved, n_rec, arr, n_traj = spectra_case(model, args, nb, seed0=seed0)
         doc = {"model": model, "args": args, "resolved": resolved, "n_records": n_rec,
-               "n_trajectories": n_traj, "spectra": arr}
+               "n_trajectories": n_traj, "seed0": seed0, "spectra": arr}
         with open(os.path.join(HERE, f"ref_spectra_{name}{extra}.json"), "w") as f:
             json.dump(doc, f)
         print("spectra", name, extra, n_rec, n_traj, flush=True)

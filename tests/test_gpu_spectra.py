@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN
-from spectra_compare import (case_chi2, compare_sections, load_reference, section_z,
+from spectra_compare import (case_chi2, chi2_bound, compare_sections, load_reference, section_z,
                              two_d_cases)
 from geliosphere_gb300 import abi, make_sim, spectra_dict
 from geliosphere_gb300.engine import records_to_log_rows, round_g, deg_rad
@@ -72,8 +72,14 @@ def test_2d_spectra_match_reference_cpu_model(engine, case):
     SolarProp grid or on the CPU models' linear grid ("_uni"), each pooled
     from three independent reference samples.  Compared: the SolarProp
     section (three LIS), the Ulysses bins and the AMS bins; per-bin mean
-    weights within Monte Carlo error, chi^2/dof <= 1.2 (case_chi2) and
-    max |z| < 3.5 over every comparison."""
+    weights within Monte Carlo error: max |z| < 3.5 over every comparison,
+    and chi^2/dof (case_chi2) below the bound a correct implementation
+    exceeds one time in 1,000 (chi2_bound: 2.01 on 29 bins).  The fixed
+    chi^2/dof <= 1.2 is printed beside it but is not a per-case gate: on 29
+    bins a correct implementation exceeds it one time in five (GPU runs of
+    the same code with eight seeds per case, against each other and against
+    the reference).  The pooled test below holds all cases together to
+    chi^2/dof <= 1.1."""
     doc, z = case_z(engine, case)
     zall = np.concatenate(list(z.values()))
     chi2 = case_chi2(z)
@@ -88,7 +94,8 @@ def test_2d_spectra_match_reference_cpu_model(engine, case):
     else:
         assert z["weber"].size >= 12 and z["ams"].size >= 5 and z["ulysses"].size >= 1
     assert np.abs(zall).max() < 3.5
-    assert max(chi2.values()) <= 1.2
+    for k, v in chi2.items():
+        assert v <= chi2_bound(z[k].size), (k, v, z[k].size)
 
 
 def test_2d_spectra_pooled_over_cases(engine):
@@ -107,7 +114,7 @@ def test_2d_spectra_pooled_over_cases(engine):
             tot[k] = (s + float(np.sum(v ** 2)), n + v.size)
     print("pooled over cases: " + "; ".join(f"{k} chi2/dof {s / n:.3f} ({n} bins)" for k, (s, n) in tot.items()))
     for k, (s, n) in tot.items():
-        assert n >= 60, k
+        assert n >= (20 if k == "ulysses" else 200), k      # ~2 Ulysses bins per case
         assert s / n <= 1.1, k
 
 

@@ -36,7 +36,14 @@ Other workloads (--workload; each prints its own line of the same form):
             weights answering 2,000 simulations x 100 grid points per step
             (the surrogate workload's query), spectra/s and tensor roofline
 
-Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gelio|reference]
+--impl reference_gpu : the reference's own 2D Geliosphere CUDA kernels
+        (built from its sources for sm_103a into oracle/_ref where the
+        sources exist) on this GPU, driven as its host code drives them, on
+        the four headline cases with its own injection grid, beside this
+        engine on the same cases (a second reference point, not the
+        driver's reference arm).
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gelio|reference|reference_gpu]
                        [--particles P] [--no-cpu-baseline] [--workload W]
 Multi-GPU (torchrun): each rank runs its own weak-scaling replica of the
 workload with its own seeds; no data-path collective.
@@ -71,7 +78,9 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="gelio", choices=["gelio", "reference"])
+    ap.add_argument("--impl", default="gelio", choices=["gelio", "reference", "reference_gpu"])
+    ap.add_argument("--ref-chunks", type=int, default=128,
+                    help="reference_gpu: 4,096-particle chunks per case of the reference kernels")
     ap.add_argument("--particles", type=int, default=None,
                     help="particles per case (default 1e7; 1e6 for the F-p workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -331,6 +340,105 @@ def run_reference_1d(args, world):
     print(json.dumps(line), flush=True)
 
 
+def run_reference_gpu(args, rank, world, local):
+    """The reference's own 2D Geliosphere CUDA kernels (GeliosphereModel.cu,
+    built from its sources for sm_103a with its own CUDA flags, loaded from
+    oracle/_ref/ref_geliosphere.cubin) on this GPU, driven as its host code
+    drives them -- 64 x 64 threads per chunk of 4,096 particles on compute
+    capability 10.3, three device synchronisations and a record copy per
+    chunk -- on the four headline cases with the reference kernel's own
+    injection (the 30-point SolarProp grid; it cannot inject the 100-point
+    log grid).  The same line carries this engine's kernels on the same four
+    cases and grid, and the Weber-section chi^2/dof of the reference
+    kernel's spectra against this engine's."""
+    if rank != 0:
+        return
+    import numpy as np
+    import torch
+    from geliosphere_gb300 import abi, Engine, make_sim
+    from geliosphere_gb300.engine import round_g, spectra_dict
+    from oracle import ffi, ref_gpu
+    if not ref_gpu.available():
+        print(json.dumps({"impl": "reference_gpu", "unavailable": "oracle/_ref/ref_geliosphere.cubin not built "
+                          "(it is compiled from the reference sources, which this host does not have)"}))
+        return
+    ffi.build()
+    torch.cuda.set_device(local)
+    eng = Engine(local)
+    chunks = args.ref_chunks
+
+    def cases(n, seed0):
+        return [make_sim(abi.GELIO_MODEL_2D_GELIOSPHERE, n, K0_cm2s=5e22, V_kms=400.0, dt=500.0, r_injection=1.0,
+                         theta_deg=90.0, tilt_deg=tilt, polarity=pol, injection=abi.GELIO_INJ_SOLARPROP_GRID,
+                         seed=seed0 + 17 * i)
+                for i, (pol, tilt) in enumerate([(1, 20.0), (1, 70.0), (-1, 20.0), (-1, 70.0)])]
+
+    ref = ref_gpu.ReferenceGeliosphere(local)
+    with ClockSampler(local) as clk:
+        ref.run(cases(ref_gpu.CHUNK, 1)[0], 1)                    # warm-up: module, curand tables
+        per_case = []
+        for sim in cases(ref_gpu.CHUNK * chunks, 1):
+            secs, rows = ref.run(sim, chunks)
+            per_case.append((secs, rows))
+    ref.close()
+    ref_traj = 4 * chunks * ref_gpu.CHUNK
+    ref_secs = sum(s for s, _ in per_case)
+    ref_value = ref_traj / ref_secs
+
+    # this engine, same cases and grid, 1e7 particles per case, through gelio_run
+    big = cases(10_000_000, 1_000_003)
+    out = (abi.Spectra * 4)()
+    eng.run(big, out=out)
+    times = []
+    for _ in range(max(1, args.steps)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = eng.run(big, out=out)
+        times.append(time.perf_counter() - t0)
+    ours = 4 * 10_000_000 * len(times) / sum(times)
+    ours_steps = int(r.stats.n_steps)
+
+    # spectra: the reference kernel's exits binned by the reference evaluator
+    # (oracle port) against this engine's spectra of 3e6 particles per case
+    chi2 = []
+    mine = eng.run(cases(3_000_000, 2_000_003))
+    for i, (_, rows) in enumerate(per_case):
+        a = spectra_dict(ffi.evaluate(abi.GELIO_MODEL_2D_GELIOSPHERE, round_g(rows)))
+        b = spectra_dict(mine.spectra[i])
+        z = []
+        for w, w2, nn in (("sp_weber", "sp_weber2", "sp_n"),):
+            na, nb = np.asarray(a[nn], float), np.asarray(b[nn], float)
+            ok = (na >= 200) & (nb >= 200)
+            ma, mb = np.asarray(a[w])[ok] / na[ok], np.asarray(b[w])[ok] / nb[ok]
+            va = (np.asarray(a[w2])[ok] / na[ok] - ma ** 2) / (na[ok] - 1)
+            vb = (np.asarray(b[w2])[ok] / nb[ok] - mb ** 2) / (nb[ok] - 1)
+            z.append((ma - mb) / np.sqrt(va + vb))
+        z = np.concatenate(z)
+        chi2.append({"bins": int(z.size), "chi2_dof": float(np.mean(z ** 2)), "max_abs_z": float(np.abs(z).max()),
+                     "exits": int(rows.shape[0])})
+    eng.close()
+    line = {
+        "metric": "2D Geliosphere trajectories/s", "value": ref_value, "unit": "trajectories/s",
+        "impl": "reference_gpu", "n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": 1e3 * ref_secs,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "2D Geliosphere, polarity +/-1 x tilt {20,70} deg, K0=5e22 cm^2/s, V=400 km/s, "
+                               "dt=500 s, r=1 AU, theta=90 deg, on the reference kernel's own injection "
+                               "(30-point SolarProp grid)",
+                   "kernels": "reference GeliosphereModel.cu built from its sources for sm_103a "
+                              "(--use_fast_math -Xptxas -O3, one translation unit), 64 blocks x 64 threads "
+                              "per 4,096-particle chunk, three device synchronisations and a record copy "
+                              "per chunk (log.dat text output not timed)",
+                   "chunks_per_case": chunks, "trajectories": ref_traj},
+        "per_case_seconds": [round(s, 4) for s, _ in per_case],
+        "gelio_same_cases": {"value": ours, "unit": "trajectories/s", "particles_per_case": 10_000_000,
+                             "particle_steps_per_s": ours_steps / (sum(times) / len(times)),
+                             "over_reference_gpu": ours / ref_value, "through": "gelio_run, host buffers"},
+        "spectra_vs_gelio": chi2,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -402,7 +510,7 @@ def run_batch256(args, eng, rank, world, local):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * sum(times) / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": workload_batch256.__doc__.replace("\n", " "), "simulations": n,
+            "config": {"workload": " ".join(workload_batch256.__doc__.split()), "simulations": n,
                        "particles": total, "graph": True,
                        "tuned": {"block": tune.block_size, "refill": tune.refill_interval} if tune else None,
                        "l2": "flushed between timed steps (256 MiB write)"},
@@ -467,7 +575,7 @@ def run_batch_cli(args, rank, world):
             "unit": "trajectories/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": run_batch_cli.__doc__.replace("\n", " "), "rows": 256, "particles": particles},
+            "config": {"workload": " ".join(run_batch_cli.__doc__.split()), "rows": 256, "particles": particles},
             "e2e": {"value": v, "unit": "trajectories/s", "h2d_bytes_per_step": 256 * 96,
                     "d2h_bytes_per_step": 256 * 64808},
             "gpu_launches": 3 * args.steps}
@@ -566,7 +674,7 @@ def run_surrogate(args, eng, rank, world, local):
     line = {"metric": "surrogate spectra/s", "value": sur_rate, "unit": "spectra/s", "n_gpus": world,
             "steps": 1, "warmup": 1, "ms_per_step": 1e3 * t_pred, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
-            "config": {"workload": run_surrogate.__doc__.replace("\n", " "),
+            "config": {"workload": " ".join(run_surrogate.__doc__.split()),
                        "train_spectra": len(train), "train_particles": args.surr_train_particles,
                        "test_draws": len(test), "test_particles": args.surr_test_particles,
                        "epochs": args.surr_epochs, "batch_rows": 8192, "members": 5, "lis": "Usoskin 2005"},
@@ -642,7 +750,7 @@ def run_surrogate_infer(args, eng, rank, world, local):
     line = {"metric": "surrogate inference spectra/s", "value": world * n / wall, "unit": "spectra/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
-            "config": {"workload": run_surrogate_infer.__doc__.replace("\n", " "), "members": members,
+            "config": {"workload": " ".join(run_surrogate_infer.__doc__.split()), "members": members,
                        "simulations": n, "rows": rows},
             "device_ms_per_step": dev_ms, "wall_over_device": 1e3 * wall / dev_ms,
             "e2e": {"value": world * n / wall, "unit": "spectra/s", "h2d_bytes_per_step": n * 96,
@@ -663,6 +771,9 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if args.impl == "gelio" else "gloo")
+    if args.impl == "reference_gpu":
+        run_reference_gpu(args, rank, world, local)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
         if world > 1:

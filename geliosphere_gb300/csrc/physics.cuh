@@ -285,6 +285,23 @@ __device__ __forceinline__ void theta_update(Lane<R> &L, R dth) {
 // ---------------------------------------------------------------------------
 // 2D Geliosphere: GeliosphereModel.cu:82-390 (Eq. 16-44 of the Geliosphere
 // model description, drifts of Kappl 2016 Eq. 26-37).
+//
+// The same equations, evaluated with shared factors so that the step issues
+// fewer FP32 instructions (the kernel is bound by instruction issue):
+//   * beta P, r^2 / sqrt(Cb), (1 - ratio) kd / Cb^2.5 and the drift prefactor
+//     P beta r gamma / Cb are formed once;
+//   * K0 beta P (Eq. 39) = 3 (5/3.4) kd, so Eq. 38-42 collapse to
+//     dKtt / r^2 = -CKtt0 (ratio kd / Cb^1.5 + 9 (5/3.4) (1 - ratio) kd rd2 / Cb^2.5)
+//     off the poles, and Eq. 44 / r = -3 dKrtr gamma^2 cot(theta);
+//   * Eq. 35-36: 2 r sqrt(Cb) - r^2 COmega / (2 sqrt(Cb)) = (2 r Cb - r^2 COmega / 2) / sqrt(Cb)
+//     (and the Cb^1.5 form likewise), so one 2 r Cb serves both;
+//   * Eq. 16: Krr Ktt - Krt^2 = Kper (Ktt + dK / Cb) exactly (Krt^2 = rd2 (dK / Cb)^2),
+//     which also removes the cancellation of the difference; sqrt(dt) goes
+//     into one factor sqrt(2 dt / Ktt) shared by B11 and B12, and B22 sqrt(dt)
+//     = Ktt sqrt(2 dt / Ktt) / r;
+//   * Eq. 23: T (T + 2 T0) / (T + T0) = P beta;
+//   * dt and 1 / r are applied once to the summed deterministic terms of dr
+//     and dtheta.
 // ---------------------------------------------------------------------------
 template <class R>
 __device__ __forceinline__ int step_geliosphere(Lane<R> &L, const Consts<R> &k, R n1, R n2, R n4) {
@@ -297,9 +314,11 @@ __device__ __forceinline__ int step_geliosphere(Lane<R> &L, const Consts<R> &k, 
   const R P = M::sqrt(T * T2);               // rigidity [GV]
   const R inv_Tp = M::rcp(Tp);
   const R beta = P * inv_Tp;
+  const R bP = beta * P;
   R s, c;
   phase_sincos(L.th, &s, &c);
   const R inv_s = M::rcp(s);
+  const R cot = c * inv_s;
   const bool polarA = (th < (R)kThetaLo) || (th > (R)kThetaHi);   // Eq. 25 branch
   const bool nonpolarB = (th > (R)kThetaLo) && (th < (R)kThetaHi);
   const R inv_rh = R(1) / (R)kRh;
@@ -310,66 +329,51 @@ __device__ __forceinline__ int step_geliosphere(Lane<R> &L, const Consts<R> &k, 
   const R gamma2 = gamma * gamma;
   const R r2 = r * r;
   const R inv_r = M::rcp(r);
-  const R inv_r2 = inv_r * inv_r;
   const R rd2 = r2 * deltarh2;
   const R Cb = R(1) + gamma2 + rd2;            // Eq. 26
   const R inv_Cb = M::rcp(Cb);
   const R sqCb = M::sqrt(Cb);
   const R isqCb = M::rcp(sqCb);
-  const R Cb15 = Cb * sqCb;
   const R inv_Cb15 = inv_Cb * isqCb;
   const R inv_Cb25 = inv_Cb15 * inv_Cb;
-  const R inv_Cb2 = inv_Cb * inv_Cb;
-  const R inv_Cb3 = inv_Cb2 * inv_Cb;
+  const R r2isq = r2 * isqCb;
   const R Pc = (P < (R)0.1f) ? (R)0.1f : P;
-  const R Kpar = k.kpar_c * beta * Pc * r2 * isqCb;   // Eq. 32
-  const R Kper = k.ratio * Kpar;                        // Eq. 33
-  const R dKp = Kpar - Kper;
-  const R Krr = Kper + dKp * inv_Cb;                    // Eq. 27
-  const R Ktt = Kper + rd2 * dKp * inv_Cb;              // Eq. 28
-  const R Krt = deltarh * dKp * r * inv_Cb;             // Eq. 29
-  const R inv_Ktt = M::rcp(Ktt);
-  const R sq2Ktt = M::sqrt(R(2) * Ktt);
-  const R B11 = M::sqrt(R(2) * (Krr * Ktt - Krt * Krt) * inv_Ktt);   // Eq. 16
-  const R B12 = Krt * inv_Ktt * sq2Ktt;                              // Eq. 17
-  const R B22 = sq2Ktt * inv_r;                                      // Eq. 18
-  const R COmega = R(2) * r * k.ov2 * s * s + R(2) * r * deltarh2;   // Eq. 34
-  const R KbR = k.K0 * beta * P;
-  const R kd = k.kd_c * beta * P;                                    // K0 beta P / (3 * 5/3.4)
-  const R dKper = k.ratio * kd * (R(2) * r * sqCb - r2 * COmega * R(0.5) * isqCb) * inv_Cb;   // Eq. 36
-  const R dKrr = dKper + k.one_m_ratio * kd * (R(2) * r * Cb15 - R(1.5) * r2 * COmega * sqCb) * inv_Cb3;  // Eq. 35
-  const R CKtt0 = s * c * k.ov2 * r2;                                // Eq. 37
-  R dKtt, dKrtt;
-  const R base = k.one_m_ratio * kd * r2 * r * inv_rh * inv_Cb25;    // Eq. 44 prefactor
+  const R Kpar = k.kpar_c * beta * Pc * r2isq;                  // Eq. 32
+  const R Kper = k.ratio * Kpar;                                // Eq. 33
+  const R dKC = (Kpar - Kper) * inv_Cb;
+  const R Krr = Kper + dKC;                                     // Eq. 27
+  const R Ktt = Kper + rd2 * dKC;                               // Eq. 28
+  const R Krt = deltarh * r * dKC;                              // Eq. 29
+  // Eq. 16-18 with sqrt(dt): B11 = sqrt(2 Kper (Ktt + dKC) / Ktt), B12 = Krt sqrt(2 / Ktt),
+  // B22 = sqrt(2 Ktt) / r
+  const R w = M::sqrt(R(2) * k.dt * M::rcp(Ktt));
+  const R noise_r = w * (n1 * M::sqrt(Kper * (Ktt + dKC)) + n2 * Krt);
+  const R noise_th = n4 * Ktt * w * inv_r;
+  const R kd = k.kd_c * bP;                                     // K0 beta P / (3 * 5/3.4)
+  const R rkd = k.ratio * kd;
+  const R okdC25 = k.one_m_ratio * kd * inv_Cb25;
+  const R tr = R(2) * r;
+  const R r2COmega = tr * r2 * (k.ov2 * s * s + deltarh2);     // r^2 COmega, Eq. 34
+  const R trCb = tr * Cb;
+  const R dKrr = rkd * (trCb - R(0.5) * r2COmega) * inv_Cb15    // Eq. 36
+               + okdC25 * (trCb - R(1.5) * r2COmega);           // Eq. 35
+  const R CKtt0 = s * c * k.ov2 * r2;                           // Eq. 37
+  const R dKrtr = okdC25 * deltarh * r2;                        // Eq. 43
+  R dKtt_r2, dKrtt_r;                                           // dKtt / r^2, dKrtt / r
   if (nonpolarB) {
-    const R dKtt1 = -k.ratio * kd * r2 * CKtt0 * inv_Cb15;           // Eq. 38
-    const R dKtt2 = k.one_m_ratio * KbR * r2 * r2 * deltarh2;         // Eq. 39
-    const R dKtt4 = R(3) * CKtt0 * inv_Cb25;                           // Eq. 41
-    dKtt = dKtt1 - dKtt2 * dKtt4;                                      // Eq. 42
-    dKrtt = -base * delta * R(3) * gamma2 * c * inv_s;
+    dKtt_r2 = -CKtt0 * (rkd * inv_Cb15 + R(9) * (R)kC53 * okdC25 * rd2);   // Eq. 38-42
+    dKrtt_r = R(-3) * dKrtr * gamma2 * cot;                               // Eq. 44
   } else {
     const R inv_s2 = inv_s * inv_s;
-    const R inv_s3 = inv_s2 * inv_s;
-    const R CKtt = CKtt0 - r2 * k.d0rh2 * c * inv_s3;
-    const R dKtt1 = -k.ratio * kd * r2 * CKtt * inv_Cb15;
-    const R dKtt2 = k.one_m_ratio * KbR * r2 * r2 * k.d0rh2;
-    const R dKtt3 = R(-2) * c * inv_s3 * k.inv_3c53 * inv_Cb15;              // Eq. 40
-    const R dKtt4 = R(3) * CKtt * inv_s2 * k.inv_3c53 * inv_Cb25;
-    dKtt = dKtt1 + dKtt2 * (dKtt3 - dKtt4);
-    dKrtt = -base * k.delta0 * c * inv_s2 * (R(1) - R(2) * rd2 + R(4) * gamma2);
+    const R cot_s2 = cot * inv_s2;                              // c / s^3
+    const R CKtt = CKtt0 - r2 * k.d0rh2 * cot_s2;
+    dKtt_r2 = -rkd * CKtt * inv_Cb15
+            - k.one_m_ratio * kd * r2 * k.d0rh2 * (R(2) * cot_s2 * inv_Cb15 + R(3) * CKtt * inv_s2 * inv_Cb25);
+    dKrtt_r = -okdC25 * r2 * (k.delta0 * inv_rh) * cot * inv_s * (R(1) - R(2) * rd2 + R(4) * gamma2);
   }
-  const R dKrtr = k.one_m_ratio * kd * deltarh * r2 * inv_Cb25;      // Eq. 43
-  const R dt = k.dt;
-  R dr = (-k.V + R(2) * Krr * inv_r + dKrr) * dt;                     // Eq. 21
-  dr += dKrtt * dt * inv_r + Krt * c * dt * inv_r * inv_s;
-  dr += (n1 * B11 + n2 * B12) * k.sqdt;
-  R dth = Ktt * c * inv_r2 * inv_s * dt + dKtt * dt * inv_r2;         // Eq. 22
-  dth += dKrtr * dt + R(2) * Krt * dt * inv_r;
-  dth += n4 * B22 * k.sqdt;
-  const R dT = -k.adv * T2 * inv_Tp * T * inv_r;                      // Eq. 23
   // Wavy current sheet drifts, Kappl 2016 Eq. 26 and 32-37.
-  const R Larmor = R(0.0225) * P * r2 * isqCb * M::rcp((R)kA);         // 0.0225 P / (A sqrt(Cb) / r^2)
-  const R xarg = k.alphaM + R(2) * (R)kPi * M::rcp(R(180)) * Larmor * inv_r;
+  // xarg = alphaM + 2 pi / 180 * Larmor / r, Larmor = 0.0225 P r^2 / (A sqrt(Cb))
+  const R xarg = k.alphaM + (R)(2.0 * 3.141592654 / 180.0 * 0.0225 / 3.4) * P * (r * isqCb);
   const R q = M::div((R)kPi, M::sin(xarg)) - R(1);
   const R ca = M::rcp(q);
   const R alphaH = M::acos(ca);
@@ -377,13 +381,19 @@ __device__ __forceinline__ int step_geliosphere(Lane<R> &L, const Consts<R> &k, 
   const R inv_alphaH = M::rcp(alphaH);
   const R arg = (R(1) - R(2) * th * M::rcp((R)kPi)) * tanH;
   const R f = M::atan(arg) * inv_alphaH;
-  const R dc = k.drift2 * P * beta * r * gamma * f * inv_Cb2;
-  const R DriftR = dc * c * inv_s;
-  const R DriftTheta = -dc * (R(2) + gamma2);
   const R fprime = -tanH * M::rcp(R(1) + arg * arg) * R(2) * M::rcp((R)kPi) * inv_alphaH;
-  const R DriftSheetR = k.drift1 * P * beta * r * gamma * fprime * inv_Cb;
-  dr += (DriftR + DriftSheetR) * dt;
-  dth += DriftTheta * dt * inv_r;
+  const R H = k.drift1 * bP * r * gamma * inv_Cb;              // drift1 P beta r gamma / Cb
+  const R dc = R(2) * H * f * inv_Cb;                          // drift2 P beta r gamma f / Cb^2
+  const R DriftR = dc * cot;
+  const R DriftTheta = -dc * (R(2) + gamma2);
+  const R DriftSheetR = H * fprime;
+  // Eq. 21-22 plus the drifts
+  const R det_r = (-k.V + dKrr + DriftR + DriftSheetR + dKrtt_r)
+                + inv_r * (R(2) * Krr + Krt * cot);
+  const R det_th = dKrtr + dKtt_r2 + inv_r * (R(2) * Krt + DriftTheta + Ktt * cot * inv_r);
+  const R dr = det_r * k.dt + noise_r;
+  const R dth = det_th * k.dt + noise_th;
+  const R dT = -k.adv * bP * inv_r;                                    // Eq. 23
   L.r.add(dr);
   theta_update(L, dth);
   L.T.add(-dT);

@@ -309,6 +309,10 @@ struct QEnt {
   unsigned slot_gbin;        // group slot (low 16 bits), grid bin + 1 (high 16 bits)
 };
 constexpr int kQueue = 64;   // entries per warp (<= 31 left + 32 pushed)
+// F-p: at most this many running trajectories in a warp whose tickets are
+// exhausted switch to normals drawn by the whole warp (>= 4 groups ahead each)
+constexpr int kCoopLanes = 8;
+static_assert(32 * 4 * sizeof(double) <= kQueue * sizeof(QEnt), "cooperative normals fit a warp's queue area");
 
 template <int MODEL>
 __device__ __forceinline__ void flush_queue(const KArgs &a, const Sink<MODEL> &sink, const QEnt *q,
@@ -603,6 +607,76 @@ __global__ void __launch_bounds__(256, MINB) k_persistent(const KArgs a) {
     constexpr int spc = StepsPerCall<MODEL>::value;
     const int win = (Prefetch<MODEL>::value && exhausted && a.refill < 64) ? 64 : a.refill;
     const uint32_t cap32 = (a.max_steps > 0xffffffffull) ? 0xffffffffu : (uint32_t)a.max_steps;
+    // F-p runs end on the latency of their longest chain: one test per step
+    // covers the rare events (a crossing record, a stop, the step cap), and a
+    // stopped lane leaves its group of four steps at once
+    auto fp_group = [&](const R *z) {
+      if constexpr (MODEL == kModelFp) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int res = step_fp(L, K, z[j]);
+          ++L.steps;
+          if (res != kContinue || L.steps >= cap32) {
+            if (res == kRecordAndContinue || res == kRecordAndStop)
+              emit_fp(a.ctl, a.records, a.record_capacity, sink, fp_crossing(L, sd, slot));
+            if (res == kRecordAndStop || res == kStop) {
+              active = false;
+              sink.add(slot, L.sim, kOffNSteps, (double)L.steps);
+            } else if (L.steps >= cap32) {
+              active = false;
+              sink.add(slot, L.sim, kOffNSteps, (double)L.steps);
+              sink.add(slot, L.sim, kOffNCapped, 1.0);
+            }
+            if (!active) break;
+          }
+        }
+      }
+    };
+    if constexpr (MODEL == kModelFp) {
+      // The tail of an F-p run: this warp's tickets are exhausted and at most
+      // kCoopLanes of its trajectories still run (often one chain of ~10^6
+      // steps).  A trajectory's normals depend only on (key, particle, group
+      // of four steps), so every lane of the warp draws one group for one of
+      // the running trajectories -- 32 / n groups ahead for each of n -- into
+      // the warp's exit-queue area (F-p queues no exits), and the running
+      // lanes then integrate those groups without drawing: a lone chain pays
+      // one warp-wide draw per 128 steps instead of one per 4 steps on its
+      // own instruction stream.  The normals are those of the per-lane draws
+      // (a lane at a window start is at a group boundary), so the results are
+      // identical.
+      const unsigned act = __ballot_sync(kFull, active);
+      const int na = __popc(act);
+      if (exhausted && na <= kCoopLanes) {
+        R *coop = reinterpret_cast<R *>(q);            // [na][G][4] normals, <= 128 entries
+        const int G = 32 / na;
+        const int jt = lane % na, gi = lane / na;     // this lane draws group gi of the jt-th running lane
+        unsigned m = act;
+        for (int t = 0; t < jt; ++t) m &= m - 1u;
+        const int src = __ffs(m) - 1;
+        const uint32_t k0 = __shfl_sync(kFull, L.key0, src);
+        const uint32_t k1 = __shfl_sync(kFull, L.key1, src);
+        const uint32_t st = __shfl_sync(kFull, L.steps, src);
+        const unsigned long long pid = __shfl_sync(kFull, L.pid, src);
+        R zz[4];
+        normals4<R>(k0, k1, st / 4u + (uint32_t)gi, kStreamSde, pid, zz);
+        if (gi < G) {
+#pragma unroll
+          for (int j = 0; j < 4; ++j) coop[(jt * G + gi) * 4 + j] = zz[j];
+        }
+        __syncwarp();
+        const int me = __popc(act & lanemask_lt());
+        for (int g = 0; g < G; ++g) {
+          if (active) {
+            R z[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) z[j] = coop[(me * G + g) * 4 + j];
+            fp_group(z);
+          }
+        }
+        __syncwarp();                                  // the buffer is drawn again next window
+        continue;
+      }
+    }
     for (int k = 0; k < win; k += spc) {
       if (active) {
         R z[4];
@@ -614,27 +688,7 @@ __global__ void __launch_bounds__(256, MINB) k_persistent(const KArgs a) {
           draw<MODEL, R>(L, z);
         }
         if constexpr (MODEL == kModelFp) {
-          // F-p runs end on the latency of their longest chain: one test per
-          // step covers the rare events (a crossing record, a stop, the step
-          // cap), and a stopped lane leaves the group at once
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const int res = step_fp(L, K, z[j]);
-            ++L.steps;
-            if (res != kContinue || L.steps >= cap32) {
-              if (res == kRecordAndContinue || res == kRecordAndStop)
-                emit_fp(a.ctl, a.records, a.record_capacity, sink, fp_crossing(L, sd, slot));
-              if (res == kRecordAndStop || res == kStop) {
-                active = false;
-                sink.add(slot, L.sim, kOffNSteps, (double)L.steps);
-              } else if (L.steps >= cap32) {
-                active = false;
-                sink.add(slot, L.sim, kOffNSteps, (double)L.steps);
-                sink.add(slot, L.sim, kOffNCapped, 1.0);
-              }
-              if (!active) break;
-            }
-          }
+          fp_group(z);
         } else {
 #pragma unroll
           for (int j = 0; j < spc; ++j) {

@@ -143,6 +143,8 @@ __device__ __forceinline__ void init_lane(Lane<R> &L, Consts<R> &K, const SimDev
   } else if constexpr (MODEL == kModelBp) {
     L.r.set((R)sd.r_inj);
     L.P.set(Math<R>::sqrt((R)Tinj * ((R)Tinj + R(2) * T0)));
+    L.Pt = L.P.v;
+    L.q = Math<R>::rsqrt(L.Pt * L.Pt + T0 * T0);
   } else {
     L.r.set((R)100.0001f);
     L.P.set(Math<R>::sqrt((R)Tinj * ((R)Tinj + R(2) * T0)));

@@ -373,15 +373,14 @@ __device__ __forceinline__ int step_geliosphere(Lane<R> &L, const Consts<R> &k, 
   }
   // Wavy current sheet drifts, Kappl 2016 Eq. 26 and 32-37.
   // xarg = alphaM + 2 pi / 180 * Larmor / r, Larmor = 0.0225 P r^2 / (A sqrt(Cb))
-  const R xarg = k.alphaM + (R)(2.0 * 3.141592654 / 180.0 * 0.0225 / 3.4) * P * (r * isqCb);
-  const R q = M::div((R)kPi, M::sin(xarg)) - R(1);
-  const R ca = M::rcp(q);
-  const R alphaH = M::acos(ca);
-  const R tanH = M::sqrt(R(1) - ca * ca) * q;                          // tan(acos(ca))
+  const R xarg = k.alphaM + (R)(2.0 * (double)kPi / 180.0 * 0.0225 / (double)kA) * P * (r * isqCb);
+  const R q = (R)kPi * M::rcp(M::sin(xarg)) - R(1);
+  const R alphaH = M::acos(M::rcp(q));
+  const R tanH = M::sqrt(q * q - R(1));                                // tan(acos(1 / q)), q > pi - 1
   const R inv_alphaH = M::rcp(alphaH);
-  const R arg = (R(1) - R(2) * th * M::rcp((R)kPi)) * tanH;
+  const R arg = (R(1) + (R)(-2.0 / (double)kPi) * th) * tanH;      // pi of the reference's FP32 constant
   const R f = M::atan(arg) * inv_alphaH;
-  const R fprime = -tanH * M::rcp(R(1) + arg * arg) * R(2) * M::rcp((R)kPi) * inv_alphaH;
+  const R fprime = (R)(-2.0 / (double)kPi) * tanH * inv_alphaH * M::rcp(R(1) + arg * arg);
   const R H = k.drift1 * bP * r * gamma * inv_Cb;              // drift1 P beta r gamma / Cb
   const R dc = R(2) * H * f * inv_Cb;                          // drift2 P beta r gamma f / Cb^2
   const R DriftR = dc * cot;
@@ -466,22 +465,20 @@ __device__ __forceinline__ int step_solarprop(Lane<R> &L, const Consts<R> &k, R 
   return (L.r.v < R(100)) ? kContinue : kStop;
 }
 
-// Kinetic energy [GeV] from rigidity [GV] without cancellation.
-template <class R>
-__device__ __forceinline__ R kinetic_from_rigidity(R P) {
-  const R T0 = (R)kT0;
-  return P * P * Math<R>::rcp(Math<R>::sqrt(T0 * T0 + P * P) + T0);
-}
-
 // ---------------------------------------------------------------------------
 // 1D B-p: OneDimensionBpModel.cu:69-140 (Eq. 5-7, 12-14).  V < 0.
 // ---------------------------------------------------------------------------
 template <class R>
 __device__ __forceinline__ int step_bp(Lane<R> &L, const Consts<R> &k, R z) {
   using M = Math<R>;
-  const R r = L.r.v, T = L.T.v;
+  const R r = L.r.v;
   const R T0 = (R)kT0;
-  const R beta0 = M::sqrt(T * (T + T0 + T0)) * M::rcp(T + T0);
+  // beta of the current T from the rigidity Pt that T was computed from and
+  // q = 1 / sqrt(Pt^2 + T0^2) = 1 / (T + T0), both carried from the previous
+  // step: sqrt(T (T + 2 T0)) / (T + T0) = Pt q in exact arithmetic.  After an
+  // undone step T, Pt and q keep the rejected values, as T does in the
+  // reference; the rigidity of Eq. 7 and 14 is the (restored) P.
+  const R beta0 = L.Pt * L.q;
   const R Rig = L.P.v;
   const Acc<R> Psave = L.P;
   const Acc<R> rsave = L.r;
@@ -490,17 +487,22 @@ __device__ __forceinline__ int step_bp(Lane<R> &L, const Consts<R> &k, R z) {
   const R Kdiff = k.K0 * beta0 * Rig;                   // Eq. 7
   const R dr = (k.V + R(2) * Kdiff * inv_r) * k.dt + z * M::sqrt(R(2) * Kdiff * k.dt);   // Eq. 13
   L.r.add(dr);
-  const R Tn = kinetic_from_rigidity(L.P.v);
+  const R Pn = L.P.v;
+  const R xn = Pn * Pn + T0 * T0;
+  const R qn = M::rsqrt(xn);
+  const R Tn = Pn * Pn * M::rcp(xn * qn + T0);          // P^2 / (sqrt(P^2 + T0^2) + T0)
   L.T.set(Tn);
-  const R beta = M::sqrt(Tn * (Tn + T0 + T0)) * M::rcp(Tn + T0);
+  L.Pt = Pn;
+  L.q = qn;
+  const R beta = Pn * qn;                               // beta of Tn
   const R rn = L.r.v;
   if (beta > (R)0.01f && Tn < R(200)) {
     if (rn > R(100) && (rn - dr) < R(100)) return kRecordAndStop;
   } else if (beta < (R)0.01f) {
     return kStop;
   }
-  if (rn < (R)0.3f) {           // reflecting inner boundary: undo r and p; T keeps
-    L.r = rsave;                 // the rejected step's value, as in the reference
+  if (rn < (R)0.3f) {           // reflecting inner boundary: undo r and p
+    L.r = rsave;
     L.P = Psave;
   }
   return (L.r.v < (R)100.0002f) ? kContinue : kStop;

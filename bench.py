@@ -255,7 +255,7 @@ def cpu_case_params(sim):
 
 
 # particles per grid point and case of one CPU sample (4 cases x 100 points)
-CPU_SAMPLE_PER_POINT = {"cpu_baseline": 32, "reference_step": 16}
+CPU_SAMPLE_PER_POINT = {"cpu_baseline": 384, "reference_step": 128}
 
 
 def cpu_baseline_sample(threads: int, per_point: int):
@@ -277,8 +277,10 @@ def cpu_sample_text(threads: int, per_point: int, ntraj: int, secs: float) -> st
 
 # bounded CPU samples of the 1D workloads: (chunks, contiguous particles per
 # chunk); chunks sit at evenly spaced offsets of the simulation, and 100
-# contiguous particles cover every point of the 100-point B-p grid
-PORT_SAMPLE_1D = {"bp": (32, 100), "fp": (100, 2000)}
+# contiguous particles cover every point of the 100-point B-p grid.  The F-p
+# sample is the whole 10^6-particle simulation (its longest chain included):
+# the CPU port runs it in well under a minute.
+PORT_SAMPLE_1D = {"bp": (32, 800), "fp": (100, 10000)}
 
 
 def cpu_port_sample_1d(sim, workload: str, threads: int):

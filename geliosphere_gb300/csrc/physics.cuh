@@ -534,15 +534,18 @@ __device__ __forceinline__ int step_fp(Lane<R> &L, const Consts<R> &k, R z) {
   const R dr = (k.V + R(2) * Kdiff * inv_r) * k.dt + z * (Pt * k.sq2K0dt * M::sqrt(q));
   L.r.add(dr);
   const R Pn = L.P.v;
-  const R xn = Pn * Pn + T0 * T0;
+  const R Pn2 = Pn * Pn;
+  const R xn = Pn2 + T0 * T0;
   const R qn = M::rsqrt(xn);
-  const R Tn = Pn * Pn * M::rcp(xn * qn + T0);          // P^2 / (sqrt(P^2 + T0^2) + T0)
+  const R Tn = Pn2 * M::rcp(xn * qn + T0);              // P^2 / (sqrt(P^2 + T0^2) + T0)
   L.T.set(Tn);
   L.Pt = Pn;                     // T keeps the rejected step's value if the step is undone below
   L.q = qn;
   const R rn = L.r.v;
   int res = kContinue;
-  if (beta > (R)0.01f && Tn < R(100)) {
+  // Tn < 100 GeV as Pn^2 < 100 (100 + 2 T0): the branch does not wait for
+  // the reciprocal of Tn (the chain of a lone trajectory is latency-bound)
+  if (beta > (R)0.01f && Pn2 < (R)(100.0 * (100.0 + 2.0 * (double)kT0))) {
     if ((rn - R(1)) / ((rn - dr) - R(1)) < R(0)) {
       res = kRecordAndContinue;
       L.rrec = (float)rn;     // the record keeps the crossing's r even if the step is undone below

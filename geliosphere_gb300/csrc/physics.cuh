@@ -62,6 +62,7 @@ template <> struct Math<float> {
   __device__ static __forceinline__ float acos(float x) { return acosf(x); }
   __device__ static __forceinline__ float atan(float x) { return atanf(x); }
   __device__ static __forceinline__ float abs(float x) { return fabsf(x); }
+  __device__ static __forceinline__ float copysign(float x, float y) { return copysignf(x, y); }
 };
 
 template <> struct Math<double> {
@@ -75,6 +76,7 @@ template <> struct Math<double> {
   __device__ static __forceinline__ double acos(double x) { return ::acos(x); }
   __device__ static __forceinline__ double atan(double x) { return ::atan(x); }
   __device__ static __forceinline__ double abs(double x) { return fabs(x); }
+  __device__ static __forceinline__ double copysign(double x, double y) { return ::copysign(x, y); }
 };
 
 // Kahan-compensated scalar: value v, running compensation c (true ~ v - c).
@@ -376,7 +378,9 @@ __device__ __forceinline__ int step_geliosphere(Lane<R> &L, const Consts<R> &k, 
   const R xarg = k.alphaM + (R)(2.0 * (double)kPi / 180.0 * 0.0225 / (double)kA) * P * (r * isqCb);
   const R q = (R)kPi * M::rcp(M::sin(xarg)) - R(1);
   const R alphaH = M::acos(M::rcp(q));
-  const R tanH = M::sqrt(q * q - R(1));                                // tan(acos(1 / q)), q > pi - 1
+  // tan(acos(1 / q)) = sqrt(1 - 1/q^2) q = sign(q) sqrt(q^2 - 1): q < 0 where the
+  // Larmor term carries xarg past pi (high rigidity near the poles)
+  const R tanH = M::copysign(M::sqrt(q * q - R(1)), q);
   const R inv_alphaH = M::rcp(alphaH);
   const R arg = (R(1) + (R)(-2.0 / (double)kPi) * th) * tanH;      // pi of the reference's FP32 constant
   const R f = M::atan(arg) * inv_alphaH;
@@ -407,6 +411,11 @@ __device__ __forceinline__ int step_geliosphere(Lane<R> &L, const Consts<R> &k, 
 // ---------------------------------------------------------------------------
 template <class R>
 __device__ __forceinline__ int step_solarprop(Lane<R> &L, const Consts<R> &k, R z0, R z1) {
+  // The same equations with shared factors, as in the 2D Geliosphere step:
+  // beta P, r^2 / sqrt(1 + gamma^2), the drift prefactor P beta r gamma / (1 + gamma^2);
+  // Eq. 44: 2 r sqrt(g1) - r^2 tmp / (2 sqrt(g1)) = (2 r g1 - r^2 tmp / 2) / sqrt(g1) (and
+  // the g1^1.5 form likewise); Eq. 18: T (T + 2 T0) / (T + T0) = P beta; dt and 1 / r applied
+  // once to the summed terms of dr and dtheta.
   using M = Math<R>;
   const R r = L.r.v, T = L.T.v;
   const R th = theta_full(L);
@@ -414,49 +423,54 @@ __device__ __forceinline__ int step_solarprop(Lane<R> &L, const Consts<R> &k, R 
   R s, c;
   phase_sincos(L.th, &s, &c);
   const R inv_s = M::rcp(s);
+  const R cot = c * inv_s;
   const R gamma = r * k.ov * s;
   const R gamma2 = gamma * gamma;
   const R Tp = T + T0;
   const R P = M::sqrt(T * (Tp + T0));
   const R beta = P * M::rcp(Tp);
+  const R bP = beta * P;
   const R g1 = R(1) + gamma2;
   const R inv_g1 = M::rcp(g1);
   const R sq1 = M::sqrt(g1);
   const R isq1 = M::rcp(sq1);
+  const R inv_g1_15 = inv_g1 * isq1;
+  const R inv_g1_25 = inv_g1_15 * inv_g1;
   const R r2 = r * r;
   const R inv_r = M::rcp(r);
-  const R tmp = R(2) * r * k.ov2 * s * s;                                       // Eq. 44
-  const R kbr = k.K0 * beta * P;
-  R dKrr = k.ratio * kbr * (R(2) * r * sq1 - r2 * tmp * R(0.5) * isq1) * inv_g1;
-  dKrr += k.one_m_ratio * kbr * (R(2) * r * g1 * sq1 - R(1.5) * r2 * tmp * sq1) * inv_g1 * inv_g1 * inv_g1;
-  dKrr = dKrr * R(5) * M::rcp(R(3) * (R)3.4f);
+  const R r2isq = r2 * isq1;
+  const R tr = R(2) * r;
+  const R r2tmp = tr * r2 * k.ov2 * s * s;                                      // r^2 tmp, Eq. 44
+  const R trg1 = tr * g1;
+  const R kbr = k.K0 * bP * (R)(5.0 / (3.0 * (double)3.4f));                   // K0 beta P 5 / (3 * 3.4)
+  const R dKrr = kbr * (k.ratio * (trg1 - R(0.5) * r2tmp) * inv_g1_15
+                        + k.one_m_ratio * (trg1 - R(1.5) * r2tmp) * inv_g1_25);
   const R Pc = (P < (R)0.1f) ? (R)0.1f : P;
-  const R Kpar = k.kpar_c * beta * Pc * r2 * isq1;                              // Eq. 42
+  const R Kpar = k.kpar_c * beta * Pc * r2isq;                                  // Eq. 42
   const R Kper = k.ratio * Kpar;                                                // Eq. 43
   const R Krr = Kper + (Kpar - Kper) * inv_g1;                                  // Eq. 14
-  const R dt = k.dt;
-  R dr = (-k.V + R(2) * Krr * inv_r + dKrr) * dt + z0 * M::sqrt(R(2) * Krr * dt);   // Eq. 16
   const R Ktt = Kper;                                                           // Eq. 15
-  R dth = Ktt * c * inv_r * inv_r * inv_s * dt * inv_g1;                        // Eq. 17
-  dth += z1 * M::sqrt(R(2) * Ktt * dt) * inv_r;
-  const R dT = -k.adv * (Tp + T0) * M::rcp(Tp) * T * inv_r;                    // Eq. 18
-  const R Larmor = R(0.0225) * P * r2 * isq1 * M::rcp((R)kA);
-  const R xarg = k.alphaM + R(2) * (R)kPi * M::rcp(R(180)) * Larmor * inv_r;
-  const R q = M::div((R)kPi, M::sin(xarg)) - R(1);
-  const R ca = M::rcp(q);
-  const R alphaH = M::acos(ca);
-  const R tanH = M::sqrt(R(1) - ca * ca) * q;
+  const R dt = k.dt;
+  // Wavy current sheet drifts (Eq. 26, 32-37), as in the 2D Geliosphere step
+  const R xarg = k.alphaM + (R)(2.0 * (double)kPi / 180.0 * 0.0225 / (double)kA) * P * (r * isq1);
+  const R q = (R)kPi * M::rcp(M::sin(xarg)) - R(1);
+  const R alphaH = M::acos(M::rcp(q));
+  const R tanH = M::copysign(M::sqrt(q * q - R(1)), q);                      // tan(acos(1 / q))
   const R inv_alphaH = M::rcp(alphaH);
-  const R arg = (R(1) - R(2) * th * M::rcp((R)kPi)) * tanH;
+  const R arg = (R(1) + (R)(-2.0 / (double)kPi) * th) * tanH;
   const R f = M::atan(arg) * inv_alphaH;
-  const R fprime = -tanH * M::rcp(R(1) + arg * arg) * R(2) * M::rcp((R)kPi) * inv_alphaH;
-  const R inv_g1sq = inv_g1 * inv_g1;
-  const R pbr = P * beta * r * gamma;
-  const R DriftR = k.drift2 * pbr * c * f * inv_g1sq * inv_s;                  // Eq. 35
-  const R DriftSheetR = k.drift1 * pbr * fprime * inv_g1;                     // Eq. 37
-  dr += (DriftR + DriftSheetR) * dt;
-  const R DriftTheta = k.dtheta_sp * pbr * (R(2) + gamma2) * f * inv_g1sq;     // Eq. 36
-  dth += DriftTheta * dt * inv_r;
+  const R fprime = (R)(-2.0 / (double)kPi) * tanH * inv_alphaH * M::rcp(R(1) + arg * arg);
+  const R H = bP * r * gamma * inv_g1;                                          // P beta r gamma / g1
+  const R D2 = H * f * inv_g1;
+  const R DriftR = k.drift2 * D2 * cot;                                         // Eq. 35
+  const R DriftSheetR = k.drift1 * H * fprime;                                  // Eq. 37
+  const R DriftTheta = k.dtheta_sp * D2 * (R(2) + gamma2);                      // Eq. 36
+  // Eq. 16-18
+  const R dr = (-k.V + dKrr + DriftR + DriftSheetR + R(2) * Krr * inv_r) * dt
+             + z0 * M::sqrt(R(2) * Krr * dt);
+  const R dth = dt * inv_r * (Ktt * cot * inv_r * inv_g1 + DriftTheta)
+              + z1 * M::sqrt(R(2) * Ktt * dt) * inv_r;
+  const R dT = -k.adv * bP * inv_r;
   L.r.add(dr);
   theta_update(L, dth);
   L.T.add(-dT);

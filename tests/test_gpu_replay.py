@@ -49,6 +49,11 @@ def cases():
                                         theta_deg=12.0, injection=abi.GELIO_INJ_SOLARPROP_GRID),
         "geliosphere_north_pole": make_sim(G, 0, dt=500, tilt_deg=20, seed=14, r_injection=5.0, theta_deg=1.0),
         "geliosphere_south_pole": make_sim(G, 0, dt=500, tilt_deg=20, seed=15, r_injection=5.0, theta_deg=179.5),
+        # 2-5 TV at 20 AU, 8 deg from the pole, tilt 70 deg: the Larmor term carries the
+        # current-sheet angle past pi, so q = pi / sin(angle) - 1 < 0 and tan(alpha_H) < 0
+        "geliosphere_high_rigidity": make_sim(G, 0, dt=500, tilt_deg=70, polarity=1, seed=16, r_injection=20.0,
+                                              theta_deg=8.0, injection=abi.GELIO_INJ_LOG_GRID, inj_min=2000,
+                                              inj_max=5000, inj_points=16),
         "solarprop": make_sim(S, 0, dt=500, polarity=1, seed=21),
         "solarprop_neg": make_sim(S, 0, dt=500, polarity=-1, seed=22, tilt_deg=30,
                                   flags=abi.GELIO_FLAG_SOLARPROP_THETA_DRIFT_POLARITY),

@@ -670,7 +670,7 @@ int infer_fused(gelio_surrogate *s, int c, float *y, long long stride) {
   a.timeout_ns = 2000000000ull;
   const int items = E * a.n_pairs;
   const int grid = std::max(1, std::min(items, s->sm_count));
-  k_mlp_infer_fused<<<grid, kGemmThreads, kFusedSmem, s->stream>>>(maps, a);
+  k_mlp_infer_fused<<<grid, kFusedThreads, kFusedSmem, s->stream>>>(maps, a);
   return cuda_status(cudaGetLastError());
 }
 
@@ -725,6 +725,8 @@ int infer_sims(gelio_surrogate *s, const gelio_sim_params *sims, int n, size_t r
   SUR_TRY(cudaMemcpyAsync(s->d_pup, s->h_pstage, up, cudaMemcpyHostToDevice, s->stream));
   k_query_sims<<<(n + 127) / 128, 128, 0, s->stream>>>(d_psims, n, d_pq);
   SUR_TRY(cudaGetLastError());
+  // the fused kernel adds the two column halves of each head output into y
+  SUR_TRY(cudaMemsetAsync(s->d_py, 0, E * stride * sizeof(float), s->stream));
   size_t padded = 0;
   for (size_t off = 0; off < rows; off += (size_t)s->qrows) {
     const int c = (int)std::min<size_t>((size_t)s->qrows, rows - off);

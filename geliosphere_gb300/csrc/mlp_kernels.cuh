@@ -396,8 +396,11 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
 //                      into that tile's TMEM accumulator (2 x 256 columns),
 //                      the tiles staggered by two chunks so that one tile's
 //                      epilogue runs under the other tile's products
-//   warps 2-9          epilogue: warp w takes TMEM lane quarter w % 4 of
-//                      tile (w - 2) / 4, all 256 columns of its 32 rows
+//   warps 2-17         epilogue: warp w takes TMEM lane quarter w % 4 of
+//                      tile ((w - 2) / 4) % 2, columns 128 ((w - 2) / 8) ..
+//                      + 127 of its 32 rows (two warps per row quarter, so
+//                      each drains half the accumulator: the epilogue is
+//                      bound by the latency of its TMEM loads)
 // Every value equals the layer-by-layer INFER / INFER_LAST path bit for bit:
 // the same operands in the same K order, the same epilogue arithmetic and
 // the head summed as (sum of columns 0-127 + b5) + sum of columns 128-255.
@@ -405,6 +408,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
 // ----------------------------------------------------------------------------
 constexpr int kFusedMaxMembers = 16;
 constexpr int kFusedStages = 2;
+constexpr int kFusedEpiWarps = 16;
+constexpr int kFusedThreads = 64 + 32 * kFusedEpiWarps;
 constexpr uint32_t kFusedA = kTileM * kWidth * 2;                 // 64 KiB: one tile's activations
 constexpr size_t kFusedSmem = 1024 + 2 * (size_t)kFusedA + kFusedStages * (size_t)kStageB + 256;
 
@@ -431,7 +436,7 @@ __device__ __forceinline__ void named_sync(int id, int count) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
 
-__global__ void __launch_bounds__(kGemmThreads, 1)
+__global__ void __launch_bounds__(kFusedThreads, 1)
     k_mlp_infer_fused(const __grid_constant__ FusedMaps maps, const FusedArgs a) {
   extern __shared__ unsigned char smem_raw[];
   __shared__ float s_b[4][kWidth], s_w5[kWidth];
@@ -457,7 +462,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     tc::mbar_init(a_empty, 1);
     for (int t = 0; t < 2; ++t) {
       tc::mbar_init(&acc_full[t], 1);
-      tc::mbar_init(&acc_empty[t], kEpiWarps / 2);
+      tc::mbar_init(&acc_empty[t], kFusedEpiWarps / 2);
     }
     tc::fence_mbar_init();
     tc::tma_prefetch(&maps.q0);
@@ -567,10 +572,11 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       }
     }
   } else {
-    const int q = warp & 3;                        // TMEM lane quarter
-    const int t = (warp - 2) >> 2;                 // tile of the pair
+    const int q = warp & 3;                        // TMEM lane quarter (a warp reaches lanes 32 (warp % 4) ..)
+    const int t = ((warp - 2) >> 2) & 1;           // tile of the pair
+    const int half = (warp - 2) >> 3;              // columns 128 half .. 128 half + 127
     const int r = q * 32 + lane;                   // row in the tile
-    const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)t * kTmemCols;
+    const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)t * kTmemCols + (uint32_t)(half * 128);
     unsigned char *arow = base + t * kFusedA + r * 128;
     uint32_t layer = 0;
     bool ok = true;
@@ -580,58 +586,62 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       const int e = w / a.n_pairs, pair = w % a.n_pairs;
       // this member's biases and head (every epilogue warp is past the
       // previous item before they are replaced)
-      named_sync(1, 32 * kEpiWarps);
+      named_sync(1, 32 * kFusedEpiWarps);
       const float *P = a.P[e];
-      for (int i = tid - 64; i < kWidth; i += 32 * kEpiWarps) {
+      for (int i = tid - 64; i < kWidth; i += 32 * kFusedEpiWarps) {
         s_b[0][i] = 0.5f * P[kOffB1 + i];          // halved: silu_infer32
         s_b[1][i] = 0.5f * P[kOffB2 + i];
         s_b[2][i] = 0.5f * P[kOffB3 + i];
         s_b[3][i] = 0.5f * P[kOffB4 + i];
         s_w5[i] = P[kOffW5 + i];
       }
-      named_sync(1, 32 * kEpiWarps);
+      named_sync(1, 32 * kFusedEpiWarps);
       for (int l = 0; l < 4; ++l, ++layer) {
         if (ok) ok = __all_sync(0xffffffffu, tc::mbar_wait(&acc_full[t], layer & 1, deadline));
         if (!ok) continue;
         tc::tc_fence_after();
-        float h0 = 0.0f, hs = 0.0f;            // head: columns 0-127, then the running half
+        float hs = 0.0f;                       // head: this warp's half of the columns
         // 32-column chunks of the accumulator, the next chunk's TMEM load in
         // flight while this one is evaluated
+        constexpr int kChunks = kWidth / 64;   // chunks of 32 columns in a half
         uint32_t buf[2][32];
         tc::tmem_ld32_issue(trow, buf[0]);
         tc::tmem_wait_ld(buf[0]);
 #pragma unroll
-        for (int c = 0; c < kWidth / 32; ++c) {
-          if (c + 1 < kWidth / 32) tc::tmem_ld32_issue(trow + (uint32_t)((c + 1) * 32), buf[(c + 1) & 1]);
-          if (c == 4) { h0 = hs; hs = 0.0f; }
+        for (int c = 0; c < kChunks; ++c) {
+          if (c + 1 < kChunks) tc::tmem_ld32_issue(trow + (uint32_t)((c + 1) * 32), buf[(c + 1) & 1]);
+          const int cc = half * kChunks + c;   // 32-column chunk of the layer
           float v[32];
 #pragma unroll
           for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(buf[c & 1][j]);
           __align__(16) __nv_bfloat16 out[32];
-          silu_infer32(v, &s_b[l][c * 32], out);
+          silu_infer32(v, &s_b[l][cc * 32], out);
           if (l == 3) {
 #pragma unroll
-            for (int j = 0; j < 32; ++j) hs += __bfloat162float(out[j]) * s_w5[c * 32 + j];
+            for (int j = 0; j < 32; ++j) hs += __bfloat162float(out[j]) * s_w5[cc * 32 + j];
           }
           if (l < 3) {
-            // columns 32c .. 32c+31 = K-chunk c / 2, 16-byte pieces 4 (c % 2) .. +3
+            // columns 32cc .. 32cc+31 = K-chunk cc / 2, 16-byte pieces 4 (cc % 2) .. +3
             const uint4 *src = reinterpret_cast<const uint4 *>(out);
-            unsigned char *chunk = arow + (c >> 1) * kStageA;
+            unsigned char *chunk = arow + (cc >> 1) * kStageA;
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-              const int piece = ((c & 1) * 4 + i) ^ (r & 7);
+              const int piece = ((cc & 1) * 4 + i) ^ (r & 7);
               *reinterpret_cast<uint4 *>(chunk + piece * 16) = src[i];
             }
           }
-          if (c + 1 < kWidth / 32) tc::tmem_wait_ld(buf[(c + 1) & 1]);
+          if (c + 1 < kChunks) tc::tmem_wait_ld(buf[(c + 1) & 1]);
         }
         if (l < 3) fence_proxy_async_smem();     // A written for the tensor core
         tc::tc_fence_before();
         __syncwarp();
         if (lane == 0) tc::mbar_arrive(&acc_empty[t]);
         if (l == 3) {
+          // y is zeroed before the launch: (columns 0-127 + b5) and columns
+          // 128-255 meet by atomic addition, (0 + x) + y == (0 + y) + x, the
+          // sum of the layer-by-layer path bit for bit
           const int row = pair * 2 * kTileM + t * kTileM + r;
-          if (row < a.M) a.y[(size_t)e * a.stride + row] = (h0 + P[kOffB5]) + hs;
+          if (row < a.M) atomicAdd(&a.y[(size_t)e * a.stride + row], half == 0 ? hs + P[kOffB5] : hs);
         }
       }
     }

@@ -250,21 +250,27 @@ def test_launch_variants_agree(engine, variant):
 
 
 @pytest.mark.parametrize("model", [abi.GELIO_MODEL_1D_BP, abi.GELIO_MODEL_1D_FP])
-@pytest.mark.parametrize("variant", ["plain", "small_blocks"])
+@pytest.mark.parametrize("variant", ["plain", "small_blocks", "plain_fp64"])
 def test_1d_launch_variants_agree(engine, model, variant):
     """The 1D persistent kernel draws each lane's next four normals ahead of
-    its steps and widens its window once the tickets run out; the spectra
-    stay those of the plain kernel and of other launch shapes."""
+    its steps, widens its window once the tickets run out, and (F-p) lets the
+    whole warp draw the normals of its last few trajectories; the spectra
+    stay those of the plain kernel and of other launch shapes, in FP32 and
+    in FP64 steps."""
     if model == abi.GELIO_MODEL_1D_BP:
         sim = make_sim(model, 40_000, dt=50, seed=21, injection=abi.GELIO_INJ_LOG_GRID, inj_points=50,
                        inj_min=0.05, inj_max=50.0)
     else:
         sim = make_sim(model, 200_000, dt=50, seed=22, injection=abi.GELIO_INJ_LOG_UNIFORM, inj_min=0.01,
                        inj_max=200.0, grid_min=0.01, grid_max=200.0, grid_bins=60)
-    a = spectra_dict(engine.run(sim).spectra[0])
+    if variant == "plain_fp64":
+        a = spectra_dict(engine.run(sim, precision=abi.GELIO_PREC_FP64).spectra[0])
+        b = spectra_dict(engine.run(sim, plain=True, precision=abi.GELIO_PREC_FP64).spectra[0])
+    else:
+        a = spectra_dict(engine.run(sim).spectra[0])
     if variant == "plain":
         b = spectra_dict(engine.run(sim, plain=True).spectra[0])
-    else:
+    elif variant == "small_blocks":
         b = spectra_dict(engine.run(sim, refill=12, block_size=128).spectra[0])
     assert a["n_records"] > 0
     _assert_same(a, b)

@@ -556,23 +556,22 @@ __device__ __forceinline__ int step_fp(Lane<R> &L, const Consts<R> &k, R z) {
   L.Pt = Pn;                     // T keeps the rejected step's value if the step is undone below
   L.q = qn;
   const R rn = L.r.v;
-  int res = kContinue;
-  // Tn < 100 GeV as Pn^2 < 100 (100 + 2 T0): the branch does not wait for
-  // the reciprocal of Tn (the chain of a lone trajectory is latency-bound)
-  if (beta > (R)0.01f && Pn2 < (R)(100.0 * (100.0 + 2.0 * (double)kT0))) {
-    if ((rn - R(1)) / ((rn - dr) - R(1)) < R(0)) {
-      res = kRecordAndContinue;
-      L.rrec = (float)rn;     // the record keeps the crossing's r even if the step is undone below
-    }
-  } else if (beta < (R)0.01f) {
-    return kStop;
-  }
-  if (rn < (R)0.1f) {           // undo r and p (T keeps the rejected step's value)
-    L.r = rsave;
-    L.P = Psave;
-  }
-  if (!(L.r.v < (R)100.0002f)) return (res == kRecordAndContinue) ? kRecordAndStop : kStop;
-  return res;
+  // The rare events as selects, not branches (a lone trajectory's chain is
+  // latency-bound and its branches stall it).  Tn < 100 GeV is tested as
+  // Pn^2 < 100 (100 + 2 T0), so the test does not wait for the reciprocal of Tn.
+  const bool window = beta > (R)0.01f && Pn2 < (R)(100.0 * (100.0 + 2.0 * (double)kT0));
+  const bool slow = !window && beta < (R)0.01f;                 // stop, the step kept
+  const bool cross = window && (rn - R(1)) / ((rn - dr) - R(1)) < R(0);
+  L.rrec = cross ? (float)rn : L.rrec;   // the record keeps the crossing's r even if the step is undone
+  const bool undo = !slow && rn < (R)0.1f;                      // undo r and p (T keeps the rejected value)
+  L.r.v = undo ? rsave.v : L.r.v;
+  L.r.c = undo ? rsave.c : L.r.c;
+  L.P.v = undo ? Psave.v : L.P.v;
+  L.P.c = undo ? Psave.c : L.P.c;
+  const bool out = !(L.r.v < (R)100.0002f);
+  const int ended = cross ? kRecordAndStop : kStop;
+  const int going = cross ? kRecordAndContinue : kContinue;
+  return slow ? kStop : (out ? ended : going);
 }
 
 }  // namespace gelio

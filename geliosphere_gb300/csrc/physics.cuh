@@ -510,16 +510,17 @@ __device__ __forceinline__ int step_bp(Lane<R> &L, const Consts<R> &k, R z) {
   L.q = qn;
   const R beta = Pn * qn;                               // beta of Tn
   const R rn = L.r.v;
-  if (beta > (R)0.01f && Tn < R(200)) {
-    if (rn > R(100) && (rn - dr) < R(100)) return kRecordAndStop;
-  } else if (beta < (R)0.01f) {
-    return kStop;
-  }
-  if (rn < (R)0.3f) {           // reflecting inner boundary: undo r and p
-    L.r = rsave;
-    L.P = Psave;
-  }
-  return (L.r.v < (R)100.0002f) ? kContinue : kStop;
+  // The rare events as selects, not branches; Tn < 200 GeV is tested as
+  // Pn^2 < 200 (200 + 2 T0).
+  const bool window = beta > (R)0.01f && Pn * Pn < (R)(200.0 * (200.0 + 2.0 * (double)kT0));
+  const bool exits = window && rn > R(100) && (rn - dr) < R(100);
+  const bool slow = !window && beta < (R)0.01f;
+  const bool undo = rn < (R)0.3f && !exits && !slow;    // reflecting inner boundary: undo r and p
+  L.r.v = undo ? rsave.v : L.r.v;
+  L.r.c = undo ? rsave.c : L.r.c;
+  L.P.v = undo ? Psave.v : L.P.v;
+  L.P.c = undo ? Psave.c : L.P.c;
+  return exits ? kRecordAndStop : ((slow || !(L.r.v < (R)100.0002f)) ? kStop : kContinue);
 }
 
 // ---------------------------------------------------------------------------

@@ -249,19 +249,30 @@ __device__ __forceinline__ void phase_sincos(const Acc<R> &ph, R *s, R *c) {
   }
 }
 
+// The reference's single reflection of theta (theta < 0 -> |theta|; theta > 2 pi
+// -> theta - 2 pi; else theta > pi -> 2 pi - theta) as selects, not branches.
+template <class R>
+__device__ __forceinline__ void reflect_theta(Acc<R> &t) {
+  R v = t.v, c = t.c;
+  const bool neg = v < R(0);
+  v = neg ? -v : v;
+  c = neg ? -c : c;
+  const bool over = v > (R)kTwoPi;
+  const bool flip = !over && v > (R)kPi;
+  const R w = over ? v - (R)kTwoPi : (R)kTwoPi - v;
+  t.v = (over || flip) ? w : v;
+  t.c = (over || flip) ? R(0) : c;
+}
+
 template <class R>
 __device__ __forceinline__ void theta_update(Lane<R> &L, R dth) {
   if constexpr (sizeof(R) == 8) {
     L.th.add(dth);
-    if (L.th.v < R(0)) L.th.negate();
-    if (L.th.v > (R)kTwoPi) { L.th.set(L.th.v - (R)kTwoPi); }
-    else if (L.th.v > (R)kPi) { L.th.set((R)kTwoPi - L.th.v); }
+    reflect_theta(L.th);
   } else {
     if (L.thn == 0.0f) {
       L.th.add(dth);
-      if (L.th.v < 0.0f) L.th.negate();
-      if (L.th.v > kTwoPi) { L.th.set(L.th.v - kTwoPi); }
-      else if (L.th.v > kPi) { L.th.set(kTwoPi - L.th.v); }
+      reflect_theta(L.th);
       if (L.th.v >= kTwoPiHi) phase_normalise(L.th, L.thn);   // runaway: switch representation
     } else {
       // an update below half an FP64 ulp of |theta| leaves theta unchanged
@@ -400,9 +411,11 @@ __device__ __forceinline__ int step_geliosphere(Lane<R> &L, const Consts<R> &k, 
   L.r.add(dr);
   theta_update(L, dth);
   L.T.add(-dT);
-  if (L.r.v < R(0)) L.r.negate();
-  if (L.r.v > R(100)) return kRecordAndStop;
-  return (L.r.v < R(100)) ? kContinue : kStop;   // NaN or r == 100 end the reference loop
+  const bool rneg = L.r.v < R(0);                // reflect r < 0 (a select, not a branch)
+  L.r.v = rneg ? -L.r.v : L.r.v;
+  L.r.c = rneg ? -L.r.c : L.r.c;
+  // NaN or r == 100 end the reference loop
+  return (L.r.v > R(100)) ? kRecordAndStop : ((L.r.v < R(100)) ? kContinue : kStop);
 }
 
 // ---------------------------------------------------------------------------
@@ -474,9 +487,10 @@ __device__ __forceinline__ int step_solarprop(Lane<R> &L, const Consts<R> &k, R 
   L.r.add(dr);
   theta_update(L, dth);
   L.T.add(-dT);
-  if (L.r.v < R(0)) L.r.negate();
-  if (L.r.v > R(100)) return kRecordAndStop;
-  return (L.r.v < R(100)) ? kContinue : kStop;
+  const bool rneg = L.r.v < R(0);
+  L.r.v = rneg ? -L.r.v : L.r.v;
+  L.r.c = rneg ? -L.r.c : L.r.c;
+  return (L.r.v > R(100)) ? kRecordAndStop : ((L.r.v < R(100)) ? kContinue : kStop);
 }
 
 // ---------------------------------------------------------------------------

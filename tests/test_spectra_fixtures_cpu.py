@@ -15,7 +15,7 @@ import itertools
 import numpy as np
 import pytest
 
-from spectra_compare import case_chi2, load_reference, load_sample, section_z, two_d_cases, EXTRA_SAMPLES
+from spectra_compare import case_chi2, chi2_bound, load_reference, load_sample, section_z, two_d_cases, EXTRA_SAMPLES
 
 CASES = two_d_cases()
 SAMPLES = ("",) + EXTRA_SAMPLES
@@ -42,6 +42,9 @@ def test_reference_samples_agree_with_each_other():
             z = section_z(docs[a], docs[b])
             zall = np.concatenate(list(z.values()))
             per_pair.append((case, a, b, max(case_chi2(z).values()), float(np.abs(zall).max())))
+            # the per-case gate of the GPU comparison accepts the reference against itself
+            for k, v in case_chi2(z).items():
+                assert v <= chi2_bound(z[k].size), (case, a, b, k, v)
             for k, v in z.items():
                 s, n = tot.get(k, (0.0, 0))
                 tot[k] = (s + float(np.sum(v ** 2)), n + v.size)
@@ -54,3 +57,15 @@ def test_reference_samples_agree_with_each_other():
         assert s / n <= 1.0, k
     assert np.all(zmax < 3.5)
     assert np.mean(chi2 <= 1.2) >= 0.8
+
+
+def test_case_chi2_bound():
+    """chi2_bound is the chi^2/dof that k standard normals exceed with
+    probability 1e-3: 2.01 on the 29 Weber bins, tighter with more bins,
+    always above the fixed 1.2 that a correct implementation exceeds one
+    time in five on 29 bins."""
+    from scipy import stats
+    assert abs(chi2_bound(29) - 2.0104) < 1e-3
+    assert chi2_bound(60) < chi2_bound(29) < chi2_bound(12)
+    assert abs(stats.chi2.sf(chi2_bound(29) * 29, 29) - 1e-3) < 1e-9
+    assert 0.2 < stats.chi2.sf(1.2 * 29, 29) < 0.22
